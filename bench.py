@@ -1,0 +1,320 @@
+"""Benchmark of the batched pentadiagonal PCR-Penta solve on GB300.
+
+Default workload: plain FP64 PCR-Penta through pcrp_solve_f64 on m=256
+systems of n=65536 rows (the reference's large-n global path), seeded
+strictly diagonally dominant bands, contiguous (reference) layout, inputs
+resident in HBM.  Prints ONE JSON line (rank 0).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--config c0|c1|c2|c3|c4] [--solver f64|mixed]
+
+Metric: Gunknowns/s = (systems x rows, all ranks) / device time per step.
+A step solves the whole batch once; it first restores the right-hand side
+with one device copy (8 B/unknown, counted in `traffic_note`) because the
+solve overwrites y.  The inputs (0.8 GB at m=256, n=65536) exceed the 129 MB
+L2, so no L2 flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference's PCR-Penta
+algorithm (oracle/, the reference has no CPU path of its own) on every host
+core, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "pcr-penta_gb300"))
+
+METRIC = "Gunknowns/s, % of 8 TB/s HBM; FP32+IR vs FP64 PCR at ≤1e-12 fwd err"
+UNIT = "Gunknowns/s"
+BYTES_PER_UNKNOWN = 56          # 5 FP64 bands + FP64 rhs read once, FP64 x written once
+
+CONFIGS = {
+    "c0": dict(m=1024, n=512, kind=0, name="plain FP64 PCR, shared-memory path, m=1024 n=512"),
+    "c1": dict(m=256, n=65536, kind=0, name="plain FP64 PCR, global tile-splitting path, m=256 n=65536"),
+    "c2": dict(m=4096, n=4096, kind=1, name="ADI convection-diffusion, m=4096 n=4096"),
+    "c4": dict(m=64, n=1 << 20, kind=2, name="weakly dominant, m=64 n=2^20"),
+}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.f is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() and args.impl == "ours" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def cpu_sample_gunk(cfg, systems: int, reps: int = 1):
+    """Oracle PCR restatement on `systems` systems of the workload, all cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import pcrp
+    m, n = systems, cfg["n"]
+    arrs = pcrp.generate(cfg["kind"], 7, m, n)
+    O.lib()
+    cores = os.cpu_count() or 1
+    best = None
+    for _ in range(reps):
+        t = time.perf_counter()
+        O.pcr(*arrs, m, n, threads=cores)
+        dt = time.perf_counter() - t
+        best = dt if best is None else min(best, dt)
+    return m * n / best / 1e9, cores, best
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the CPU restatement of the reference algorithm on the host cores."""
+    if rank != 0:
+        return
+    cfg = CONFIGS[args.config]
+    systems = max(1, min(cfg["m"], args.ref_systems))
+    vals = []
+    cores = os.cpu_count() or 1
+    for k in range(args.warmup + args.steps):
+        v, cores, dt = cpu_sample_gunk(cfg, systems)
+        if k >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    sample = f"{systems} of {cfg['m']} systems (n={cfg['n']}) per step, {cores} host threads"
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": cfg["m"] * cfg["n"] / value / 1e6,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded counter-based generator)", "impl": "reference",
+        "config": {"workload": cfg["name"], "m": cfg["m"], "n": cfg["n"], "layout": "contiguous",
+                   "solver": "CPU restatement of the reference PCR-Penta (oracle/pcrp_oracle.c)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local, pg):
+    import torch
+    import pcrp
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cfg = CONFIGS[args.config]
+    m, n = cfg["m"], cfg["n"]
+    stream = torch.cuda.Stream(device=dev)
+    hbm, peak_kind = peaks()
+
+    # inputs: this rank's shard of systems (weak scaling: m systems per GPU)
+    seed = 7 + rank
+    arrs = [torch.empty(m * n, dtype=torch.float64, device=dev) for _ in range(6)]
+    with torch.cuda.stream(stream):
+        pcrp.generate_device(cfg["kind"], seed, m, n, pcrp.CONTIGUOUS, arrs, stream=stream)
+        rhs = arrs[5].clone()
+    stream.synchronize()
+    solve = (lambda: pcrp.solve_f64(*arrs, m, n, stream=stream)) if args.solver == "f64" else \
+        (lambda: pcrp.solve_mixed(*arrs, m, n, stream=stream, report=False))
+
+    def step():
+        arrs[5].copy_(rhs, non_blocking=True)
+        solve()
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    stream.synchronize()
+    launches0 = pcrp.kernel_launches()
+    barrier()
+    torch.cuda.synchronize(dev)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        time.sleep(0.3)
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for _ in range(args.steps):
+                step()
+            ev1.record(stream)
+        ev1.synchronize()
+        time.sleep(0.1)
+    torch.cuda.synchronize(dev)
+    barrier()
+    launches = pcrp.kernel_launches() - launches0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if pg is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev if pg.get_backend() == "nccl" else "cpu")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * m * n / (ms * 1e-3) / 1e9
+
+    # kernel-only time of one solve (no RHS restore), for the roofline
+    ek0 = torch.cuda.Event(enable_timing=True)
+    ek1 = torch.cuda.Event(enable_timing=True)
+    kms = []
+    with torch.cuda.stream(stream):
+        for _ in range(max(3, args.steps)):
+            arrs[5].copy_(rhs, non_blocking=True)
+            ek0.record(stream)
+            solve()
+            ek1.record(stream)
+            ek1.synchronize()
+            kms.append(ek0.elapsed_time(ek1))
+    kms_med = statistics.median(kms)
+    achieved = BYTES_PER_UNKNOWN * m * n / (kms_med * 1e-3) / 1e9
+
+    # end to end through the public API with host buffers (pinned)
+    h_in = [torch.empty(m * n, dtype=torch.float64, pin_memory=True) for _ in range(6)]
+    pcrp.generate_into(cfg["kind"], seed, m, n, pcrp.CONTIGUOUS, h_in)
+    h_out = torch.empty(m * n, dtype=torch.float64, pin_memory=True)
+    e_steps = max(2, min(args.steps, 5))
+
+    def e2e_step():
+        for d, h in zip(arrs, h_in):
+            d.copy_(h, non_blocking=True)
+        solve()
+        h_out.copy_(arrs[5], non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        e2e_step()
+    stream.synchronize()
+    barrier()
+    ee0 = torch.cuda.Event(enable_timing=True)
+    ee1 = torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        ee0.record(stream)
+        for _ in range(e_steps):
+            e2e_step()
+        ee1.record(stream)
+    ee1.synchronize()
+    e_ms = ee0.elapsed_time(ee1) / e_steps
+    if pg is not None:
+        t = torch.tensor([e_ms], dtype=torch.float64, device=dev if pg.get_backend() == "nccl" else "cpu")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e_ms = float(t.item())
+    e2e_val = world * m * n / (e_ms * 1e-3) / 1e9
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.solver == "f64" else "f32+f64",
+        "data": "synthetic (seeded counter-based generator, generated on device)",
+        "config": {"workload": cfg["name"], "m": m, "n": n, "layout": "contiguous",
+                   "solver": "pcrp_solve_f64 (bit-faithful PCR-Penta)" if args.solver == "f64"
+                   else "pcrp_solve_mixed (FP32 block PCR + FP64 refinement)",
+                   "l2": "inputs larger than L2 (0.8 GB vs 129 MB), no flush",
+                   "parallelism": f"replicas x{world} (independent systems per GPU)"},
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 6 * 8 * m * n,
+                "d2h_bytes_per_step": 8 * m * n, "ms_per_step": e_ms},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None,
+                     "note": f"algorithmic {BYTES_PER_UNKNOWN} B/unknown over the solve's kernel time "
+                             f"({kms_med:.3f} ms); peak {peak_kind}"},
+        "clocks": clk.summary(),
+    }
+    if args.cpu_baseline and world == 1:
+        v, cores, dt = cpu_sample_gunk(cfg, min(m, args.ref_systems))
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{min(m, args.ref_systems)} of {m} systems (n={n}), "
+                                          f"oracle PCR restatement, {dt:.2f} s wall"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="c1")
+    ap.add_argument("--solver", choices=["f64", "mixed"], default="f64")
+    ap.add_argument("--ref-systems", type=int, default=32)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

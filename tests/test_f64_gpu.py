@@ -1,0 +1,142 @@
+"""GPU parity of the faithful FP64 PCR-Penta path against the oracle.
+
+The CUDA kernels form every product, sum and quotient of the reference's
+stride arithmetic (kernel.cu:63-153) in its order without FMA contraction,
+so the bar is BIT-EXACT equality with the CPU restatement, on every size,
+layout and pass plan, including garbage in out-of-range band slots."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+import pcrp
+from helpers import assert_bitexact, dd_bands, gpu_f64, to_device, to_layout
+
+pytestmark = pytest.mark.gpu
+
+SMALL_N = [1, 2, 3, 4, 5, 7, 8, 16, 31, 32, 33, 64, 100, 127, 128, 255, 256, 500, 512, 513, 1000, 1023, 1024]
+
+
+@pytest.mark.parametrize("n", SMALL_N)
+@pytest.mark.parametrize("layout", [pcrp.CONTIGUOUS, pcrp.INTERLEAVED])
+def test_small_path_bitexact(cuda, n, layout):
+    rng = np.random.default_rng(1000 + n)
+    m = 5
+    arrs = to_layout(dd_bands(rng, m, n, garbage=(n % 2 == 1)), m, n, layout)
+    x, _ = gpu_f64(arrs, m, n, layout, path="small")
+    assert_bitexact(x, O.pcr(*arrs, m, n, layout), f"small n={n} layout={layout}")
+
+
+@pytest.mark.parametrize("n,opts", [
+    (1025, {}), (2048, {}), (3000, {}), (4096, {}), (5001, {}),
+    (4096, dict(fuse_strides=1)), (4096, dict(fuse_strides=2, tile_rows=100)),
+    (4096, dict(smem_rows=64, fuse_strides=3, tile_rows=37)),
+    (8192, dict(smem_rows=2048)), (8192, dict(smem_rows=256, fuse_strides=4)),
+    (3000, dict(smem_rows=16, fuse_strides=5, tile_rows=300, threads=64)),
+])
+@pytest.mark.parametrize("layout", [pcrp.CONTIGUOUS, pcrp.INTERLEAVED])
+def test_split_path_bitexact(cuda, n, opts, layout):
+    rng = np.random.default_rng(n + len(opts))
+    m = 3
+    arrs = to_layout(dd_bands(rng, m, n, garbage=True), m, n, layout)
+    x, _ = gpu_f64(arrs, m, n, layout, path="split", opts=pcrp.Opts(**opts) if opts else None)
+    assert_bitexact(x, O.pcr(*arrs, m, n, layout), f"split n={n} {opts} layout={layout}")
+
+
+@pytest.mark.parametrize("n,opts", [(300, dict(smem_rows=32)), (777, dict(smem_rows=8, fuse_strides=2, tile_rows=11))])
+def test_auto_path_with_small_tiles_bitexact(cuda, n, opts):
+    """pcrp_solve_f64 may split systems below 1024 rows when told to; same bits."""
+    rng = np.random.default_rng(n)
+    m = 4
+    arrs = dd_bands(rng, m, n)
+    x, _ = gpu_f64(arrs, m, n, opts=pcrp.Opts(**opts))
+    assert_bitexact(x, O.pcr(*arrs, m, n), f"auto n={n} {opts}")
+
+
+def test_small_config_full_size_bitexact(cuda):
+    """Plain FP64 shared-memory path at m=1024, n=512 (dominant generator)."""
+    m, n = 1024, 512
+    arrs = pcrp.generate(pcrp.GEN_DOMINANT, 2024, m, n)
+    x, _ = gpu_f64(arrs, m, n)
+    assert_bitexact(x, O.pcr(*arrs, m, n), "m=1024 n=512")
+    # the reference algorithm itself is this far from elimination (5.3e-10 observed)
+    assert O.fwd_err(x, O.ge(*arrs, m, n), m, n) < 1e-8
+
+
+def test_large_config_full_size_bitexact(cuda):
+    """Plain FP64 global path at m=256, n=65536: every system bit-exact."""
+    m, n = 256, 65536
+    arrs = pcrp.generate(pcrp.GEN_DOMINANT, 7, m, n)
+    x, _ = gpu_f64(arrs, m, n)
+    assert_bitexact(x, O.pcr(*arrs, m, n), "m=256 n=65536")
+
+
+def test_max_size_bitexact(cuda):
+    """n = 2^20 (the HBM-filling size; beyond the reference's own n <= 2^19 range)."""
+    m, n = 2, 1 << 20
+    arrs = pcrp.generate(pcrp.GEN_WEAK, 11, m, n)
+    x, _ = gpu_f64(arrs, m, n)
+    assert_bitexact(x, O.pcr(*arrs, m, n), "n=2^20 weak")
+
+
+def test_adi_and_toeplitz_bitexact(cuda):
+    for kind, m, n in ((pcrp.GEN_ADI, 64, 4096), (pcrp.GEN_TOEPLITZ, 3, 256), (pcrp.GEN_TOEPLITZ, 3, 1024),
+                       (pcrp.GEN_TOEPLITZ, 2, 4096)):
+        arrs = pcrp.generate(kind, 5, m, n)
+        x, _ = gpu_f64(arrs, m, n)
+        assert_bitexact(x, O.pcr(*arrs, m, n), f"kind={kind} n={n}")
+
+
+def test_bands_are_not_modified(cuda):
+    import torch
+    for n in (300, 5000):
+        m = 3
+        arrs = dd_bands(np.random.default_rng(n), m, n)
+        t = to_device(arrs, cuda)
+        before = [v.clone() for v in t[:5]]
+        pcrp.solve_f64(*t, m, n)
+        torch.cuda.synchronize()
+        for u, v in zip(before, t[:5]):
+            assert torch.equal(u, v)
+
+
+def test_caller_workspace_and_stream(cuda):
+    import torch
+    m, n = 4, 9000
+    arrs = dd_bands(np.random.default_rng(3), m, n)
+    need = pcrp.workspace_size(m, n)
+    assert need > 0
+    small = torch.empty(need // 8 - 1, dtype=torch.float64, device=cuda)
+    t = to_device(arrs, cuda)
+    with pytest.raises(pcrp.PcrpError) as ei:
+        pcrp.solve_f64(*t, m, n, opts=pcrp.Opts(workspace=small.data_ptr(), workspace_bytes=small.numel() * 8))
+    assert ei.value.status == 3
+    ws = torch.empty(need // 8, dtype=torch.float64, device=cuda)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        t = to_device(arrs, cuda)
+        pcrp.solve_f64(*t, m, n, opts=pcrp.Opts(workspace=ws.data_ptr(), workspace_bytes=need), stream=s)
+    s.synchronize()
+    assert_bitexact(t[5].cpu().numpy(), O.pcr(*arrs, m, n), "caller workspace")
+
+
+def test_repeat_calls_are_deterministic(cuda):
+    m, n = 8, 3000
+    arrs = dd_bands(np.random.default_rng(4), m, n)
+    x1, _ = gpu_f64(arrs, m, n)
+    x2, _ = gpu_f64(arrs, m, n)
+    assert np.array_equal(x1, x2)
+
+
+def test_device_generator_matches_host(cuda):
+    import torch
+    for kind in range(4):
+        for layout in (pcrp.CONTIGUOUS, pcrp.INTERLEAVED):
+            m, n = 6, 1111
+            host = pcrp.generate(kind, 99, m, n, layout)
+            dev = [torch.empty(m * n, dtype=torch.float64, device=cuda) for _ in range(6)]
+            pcrp.generate_device(kind, 99, m, n, layout, dev)
+            torch.cuda.synchronize()
+            for h, d in zip(host, dev):
+                assert np.array_equal(h, d.cpu().numpy())
