@@ -118,6 +118,21 @@ pcrp_status pcrp_solve_f64_split(const double* a, const double* b, const double*
                                  int64_t m, int64_t n, int32_t layout,
                                  const pcrp_opts* opts, pcrp_stream stream);
 
+/* The pcrp_solve_f64 solve for callers that must not allocate device memory
+ * (host callbacks and plugin hooks that may not enter the CUDA allocator,
+ * hosts whose GPU memory is fixed at start-up).  Its scratch is a 64 MiB
+ * array compiled into the library, which every GPU that loads the library
+ * keeps until the process exits; a call therefore accepts at most
+ * m*n <= 524288 unknowns and returns PCRP_EINVAL, with the limit in the error
+ * text, for more.  It calls no allocator.  The first call on a device looks up
+ * the array's device address, so make one call per device before any stream
+ * capture.  Calls share the array: calls whose GPU work overlaps in time race
+ * on it, so order them on one stream.  Results are bit-identical to
+ * pcrp_solve_f64.  No counterpart in the reference. */
+pcrp_status pcrp_solve_f64_noalloc(const double* a, const double* b, const double* c,
+                                   const double* d, const double* e, double* y,
+                                   int64_t m, int64_t n, int32_t layout, pcrp_stream stream);
+
 /* ------------------------------------------------------------------------ */
 /* Mixed precision: FP32 PCR + FP64 iterative refinement                    */
 /* ------------------------------------------------------------------------ */

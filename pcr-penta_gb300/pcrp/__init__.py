@@ -72,6 +72,7 @@ _SIGS = {
     "pcrp_solve_f64": [_vp] * 6 + [_i64, _i64, _i32, _vp, _vp],
     "pcrp_solve_f64_small": [_vp] * 6 + [_i64, _i64, _i32, _vp, _vp],
     "pcrp_solve_f64_split": [_vp] * 6 + [_i64, _i64, _i32, _vp, _vp],
+    "pcrp_solve_f64_noalloc": [_vp] * 6 + [_i64, _i64, _i32, _vp],
     "pcrp_solve_mixed": [_vp] * 6 + [_i64, _i64, _i32, ctypes.c_double, _i32, _vp, _vp, _vp],
     "pcrp_residual_f64": [_vp] * 8 + [_i64, _i64, _i32, _vp],
     "pcrp_solve_ragged": [_vp] * 6 + [_vp, _i64, _i64, _i32, ctypes.c_double, _i32, _vp, _vp],
@@ -164,6 +165,13 @@ def solve_f64(a, b, c, d, e, y, m: int, n: int, layout: int = CONTIGUOUS,
     rc = getattr(lib(), fn)(*[_ptr(v) for v in (a, b, c, d, e, y)], m, n, layout,
                             _opts(opts), _stream(stream))
     _check(rc, fn)
+
+
+def solve_f64_noalloc(a, b, c, d, e, y, m: int, n: int, layout: int = CONTIGUOUS, stream=None) -> None:
+    """pcrp_solve_f64 without any device allocation (scratch is a fixed array
+    inside the library; m*n <= 524288)."""
+    rc = lib().pcrp_solve_f64_noalloc(*[_ptr(v) for v in (a, b, c, d, e, y)], m, n, layout, _stream(stream))
+    _check(rc, "pcrp_solve_f64_noalloc")
 
 
 def solve_mixed(a, b, c, d, e, y, m: int, n: int, layout: int = CONTIGUOUS, tol: float = 1e-12,
