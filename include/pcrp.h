@@ -67,7 +67,8 @@ typedef struct pcrp_opts {
     int32_t  fuse_strides;     /* PCR strides fused per global-memory pass (n > smem_rows)   */
     int32_t  tile_rows;        /* rows written per CTA in a global pass                      */
     int32_t  threads;          /* threads per CTA                                            */
-    int32_t  reserved0;
+    int32_t  reserved0;        /* 0; 0x7E57 makes pcrp_solve_ragged's first dependency wait
+                                  unsatisfiable (bounded, ~4 ms) to test PCRP_ETIMEOUT       */
     void*    workspace;        /* caller-provided device scratch, or NULL                    */
     size_t   workspace_bytes;
 } pcrp_opts;

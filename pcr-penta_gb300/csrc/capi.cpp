@@ -92,9 +92,14 @@ struct F64Plan {
     int smem_rows, fuse, tile_rows, threads;
 };
 
-F64Plan f64_plan(const pcrp_opts* o)
+F64Plan f64_plan(const pcrp_opts* o, int64_t n)
 {
-    F64Plan p{PCRP_TUNED_SMEM_ROWS, PCRP_TUNED_FUSE_STRIDES, PCRP_TUNED_TILE_ROWS, PCRP_TUNED_THREADS};
+    // tuned defaults by system size (the last row covers everything larger)
+    static const int64_t table[][5] = PCRP_TUNED_F64_TABLE;
+    const int rows = (int)(sizeof(table) / sizeof(table[0]));
+    int t = 0;
+    while (t + 1 < rows && n > table[t][0]) t++;
+    F64Plan p{(int)table[t][1], (int)table[t][2], (int)table[t][3], (int)table[t][4]};
     if (o && o->size >= sizeof(pcrp_opts)) {
         if (o->smem_rows > 0) p.smem_rows = o->smem_rows;
         if (o->fuse_strides > 0) p.fuse = o->fuse_strides;
@@ -118,6 +123,8 @@ static int split_strides(int64_t n, int smem_rows)
     while (s < ns && ceil_div(n, int64_t(1) << s) > smem_rows) s++;
     return s;
 }
+
+size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_sweeps, bool info);
 
 size_t f64_workspace_bytes(int64_t m, int64_t n, int32_t layout, const F64Plan& pl, bool split)
 {
@@ -145,7 +152,7 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
     if (n > (int64_t(1) << 31) || m > (int64_t(1) << 40))
         return set_error(PCRP_EINVAL, "%s: size out of range", who);
 
-    F64Plan pl = f64_plan(o);
+    F64Plan pl = f64_plan(o, n);
     if (force_small && pl.smem_rows < n) pl.smem_rows = (int)n;         // the n <= 1024 path is one tile
     if (force_split && pl.smem_rows >= n) pl.smem_rows = 1024;         // the n > 1024 path splits
     const int ns = ref_strides(n);
@@ -239,9 +246,10 @@ pcrp_status pcrp_workspace_size(int64_t m, int64_t n, int32_t layout, int32_t wh
     *bytes = 0;
     if (m < 0 || n < 0) return set_error(PCRP_EINVAL, "pcrp_workspace_size: negative size");
     if (!valid_layout(layout)) return set_error(PCRP_EINVAL, "pcrp_workspace_size: bad layout %d", layout);
-    const F64Plan pl = f64_plan(opts);
+    const F64Plan pl = f64_plan(opts, n);
     switch (which) {
     case 0: *bytes = f64_workspace_bytes(m, n, layout, pl, true); return PCRP_OK;
+    case 1: *bytes = mixed_workspace_bytes(m, n, opts, 64, true); return PCRP_OK;
     default: return set_error(PCRP_EINVAL, "pcrp_workspace_size: unknown entry family %d", which);
     }
 }

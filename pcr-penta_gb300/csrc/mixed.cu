@@ -1,0 +1,582 @@
+// mixed.cu -- mixed-precision solve: FP32 2x2-block PCR + FP64 iterative
+// refinement, and the fused FP64 pentadiagonal residual.
+//
+// Why blocks.  The reference's scalar PCR-Penta eliminates with off-diagonal
+// pivots (alpha = -a[i]/b[i-2d], kernel.cu:73), which amplifies rounding by
+// 1/|pivot|: in FP32 it loses 3-4 digits on diagonally dominant inputs, and
+// an exactly zero off-diagonal breaks it outright.  Grouping rows in pairs
+// turns the pentadiagonal matrix into a block-tridiagonal one with 2x2
+// blocks; block PCR then pivots on the 2x2 diagonal blocks, which stay
+// well conditioned for dominant systems (block cyclic reduction preserves
+// block dominance and squares the coupling every stride), so the FP32 solve
+// keeps ~7 digits and one refinement sweep usually reaches 1e-13.
+//
+// Block row k holds rows 2k, 2k+1 and reads L_k X_{k-d} + X_k + U_k X_{k+d}
+// = Y_k after normalisation by its diagonal block (D = I).  One stride:
+//     D' = I - L_k U_{k-d} - U_k L_{k+d},  L' = -L_k L_{k-d},
+//     U' = -U_k U_{k+d},  Y' = Y_k - L_k Y_{k-d} - U_k Y_{k+d},
+// then L, U, Y <- D'^{-1} (L', U', Y').  Strides stop early once every
+// |L|,|U| entry of a system is below kTrunc (the couplings then change X by
+// less than kTrunc*|X|, far below FP32 resolution) -- truncated PCR.
+//
+// FP64 budget.  GB300 issues FP64 at ~1/64 of the FP32 rate, so FP64 is kept
+// to the residual (5 DFMA per row) and the correction (1 DADD per row).  Row
+// scaling by the main diagonal is done by powers of two in the integer
+// pipe, and every FP64<->FP32 conversion here is integer bit arithmetic
+// (no F2F instructions, which also issue on the FP64 pipe).
+//
+// Stopping rule.  With dx_s the correction of sweep s, the contraction
+// rho = |dx_s| / |dx_{s-1}| bounds the error left after applying dx_s by
+// about rho/(1-rho)*|dx_s|; a system is done when rho < 0.5 and twice that
+// bound is <= tol*|x|.
+// Each kernel reads the per-system norms left by the previous kernel, so the
+// decision needs no host round trip; finished systems skip all later work.
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+
+#include "pcrp_internal.h"
+#include "mixed_internal.h"
+
+namespace pcrp {
+namespace {
+
+constexpr float kTrunc = 1e-10f;
+constexpr int kMpThreads = 256;
+
+// ---------------------------------------------------------------------------
+// integer-pipe conversions
+// ---------------------------------------------------------------------------
+
+// Exponent e of |v| in [2^e, 2^(e+1)); 0 for zero, subnormal, inf, nan.
+__device__ __forceinline__ int d_exponent(double v) {
+    const int E = (int)((__double_as_longlong(v) >> 52) & 0x7FF);
+    return (E == 0 || E == 0x7FF) ? 0 : E - 1023;
+}
+
+// (float)(v * 2^-sh), rounded to nearest (ties away), flushing results below
+// FLT_MIN to zero and saturating to inf; integer arithmetic only.
+__device__ __forceinline__ float d2f_scaled(double v, int sh) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    const unsigned sign = (unsigned)(bits >> 63) << 31;
+    const int E = (int)((bits >> 52) & 0x7FF);
+    if (E == 0) return __uint_as_float(sign);                      // zero / subnormal
+    if (E == 0x7FF) {                                               // inf / nan
+        const unsigned nan = (bits & 0xFFFFFFFFFFFFFULL) ? 0x400000u : 0u;
+        return __uint_as_float(sign | 0x7F800000u | nan);
+    }
+    const int F = E - sh - 1023 + 127;
+    if (F <= 0) return __uint_as_float(sign);
+    if (F >= 255) return __uint_as_float(sign | 0x7F800000u);
+    const unsigned long long mant = bits & 0xFFFFFFFFFFFFFULL;
+    unsigned u = ((unsigned)F << 23) + (unsigned)(mant >> 29) + (unsigned)((mant >> 28) & 1);
+    if (u >= 0x7F800000u) u = 0x7F800000u;
+    return __uint_as_float(sign | u);
+}
+
+// Exact (double)f for normal floats; subnormals flush to zero.
+__device__ __forceinline__ double f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    const unsigned E = (u >> 23) & 0xFF;
+    if (E == 0) return __longlong_as_double((long long)sign);
+    if (E == 0xFF) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ULL |
+                                                           ((unsigned long long)(u & 0x7FFFFF) << 29)));
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(E - 127 + 1023) << 52) |
+                                            ((unsigned long long)(u & 0x7FFFFF) << 29)));
+}
+
+__device__ __forceinline__ void atomic_max_pos(unsigned* addr, float v) {
+    // non-negative floats order like their bit patterns
+    if (v > 0.0f) atomicMax(addr, __float_as_uint(v));
+    else if (!(v >= 0.0f)) atomicMax(addr, 0x7FC00000u);   // nan poisons the norm
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// 2x2 helpers (row-major m[0] m[1] / m[2] m[3])
+// ---------------------------------------------------------------------------
+struct M2 { float m0, m1, m2, m3; };
+
+__device__ __forceinline__ M2 mmul(const M2& A, const M2& B) {
+    return {fmaf(A.m0, B.m0, A.m1 * B.m2), fmaf(A.m0, B.m1, A.m1 * B.m3),
+            fmaf(A.m2, B.m0, A.m3 * B.m2), fmaf(A.m2, B.m1, A.m3 * B.m3)};
+}
+
+__device__ __forceinline__ M2 minv(const M2& D) {
+    const float det = fmaf(D.m0, D.m3, -D.m1 * D.m2);
+    const float r = __fdividef(1.0f, det);
+    return {D.m3 * r, -D.m1 * r, -D.m2 * r, D.m0 * r};
+}
+
+// The FP32 row-scaled diagonal block and couplings of block row k (rows
+// i0 = 2k, i1 = 2k+1) of a system with n rows.  Row i1 = n (odd n) is a
+// dummy identity row.  Bands are read through (base, rs).
+struct BlockRow { M2 D, L, U; int sh0, sh1; };
+
+__device__ __forceinline__ BlockRow load_block(const double* __restrict__ a, const double* __restrict__ b,
+                                               const double* __restrict__ c, const double* __restrict__ d,
+                                               const double* __restrict__ e, int64_t base, int64_t rs,
+                                               int64_t i0, int64_t n) {
+    BlockRow B;
+    const int64_t i1 = i0 + 1;
+    const int64_t g0 = base + i0 * rs, g1 = base + i1 * rs;
+    const double c0 = c[g0];
+    B.sh0 = d_exponent(c0);
+    const float a0 = i0 >= 2 ? d2f_scaled(a[g0], B.sh0) : 0.0f;
+    const float b0 = i0 >= 1 ? d2f_scaled(b[g0], B.sh0) : 0.0f;
+    const float d0 = i0 + 1 < n ? d2f_scaled(d[g0], B.sh0) : 0.0f;
+    const float e0 = i0 + 2 < n ? d2f_scaled(e[g0], B.sh0) : 0.0f;
+    const float cf0 = d2f_scaled(c0, B.sh0);
+    float a1 = 0.0f, b1 = 0.0f, cf1 = 1.0f, d1 = 0.0f, e1 = 0.0f;
+    B.sh1 = 0;
+    if (i1 < n) {
+        const double c1 = c[g1];
+        B.sh1 = d_exponent(c1);
+        a1 = d2f_scaled(a[g1], B.sh1);                         // i1 >= 1, a is in range for i1 >= 2
+        if (i1 < 2) a1 = 0.0f;
+        b1 = d2f_scaled(b[g1], B.sh1);
+        cf1 = d2f_scaled(c1, B.sh1);
+        d1 = i1 + 1 < n ? d2f_scaled(d[g1], B.sh1) : 0.0f;
+        e1 = i1 + 2 < n ? d2f_scaled(e[g1], B.sh1) : 0.0f;
+    }
+    B.D = {cf0, d0, b1, cf1};
+    B.L = {a0, b0, 0.0f, a1};
+    B.U = {e0, 0.0f, d1, e1};
+    return B;
+}
+
+// ---------------------------------------------------------------------------
+// prep: level-0 normalised block state and the first right-hand side
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMpThreads)
+mp_prep_kernel(MpArgs p)
+{
+    const int64_t nb = (p.n + 1) / 2;
+    const int64_t total = p.m * nb;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = q / nb, k = q - j * nb;
+        const int64_t base = j * p.ss;
+        const BlockRow B = load_block(p.a, p.b, p.c, p.d, p.e, base, p.rs, 2 * k, p.n);
+        const M2 Mi = minv(B.D);
+        const M2 L = mmul(Mi, B.L), U = mmul(Mi, B.U);
+        const float y0 = d2f_scaled(p.y[base + 2 * k * p.rs], B.sh0);
+        const float y1 = 2 * k + 1 < p.n ? d2f_scaled(p.y[base + (2 * k + 1) * p.rs], B.sh1) : 0.0f;
+        float* s = p.S0;
+        const int64_t T = total;
+        s[0 * T + q] = L.m0; s[1 * T + q] = L.m1; s[2 * T + q] = L.m2; s[3 * T + q] = L.m3;
+        s[4 * T + q] = U.m0; s[5 * T + q] = U.m1; s[6 * T + q] = U.m2; s[7 * T + q] = U.m3;
+        p.R[q] = fmaf(Mi.m0, y0, Mi.m1 * y1);
+        p.R[T + q] = fmaf(Mi.m2, y0, Mi.m3 * y1);
+    }
+    if (blockIdx.x == 0) {
+        for (int64_t j = threadIdx.x; j < p.m; j += blockDim.x) {
+            p.fin[j] = 0; p.status[j] = 0; p.est[j] = 0.0f;
+        }
+        for (int64_t q = threadIdx.x; q < (int64_t)kMpMaxPasses * p.m; q += blockDim.x) p.trunc[q] = 0u;
+        for (int64_t q = threadIdx.x; q < (int64_t)(p.max_sweeps + 1) * p.m; q += blockDim.x) {
+            p.ndx[q] = 0u; p.nx[q] = 0u;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 block PCR pass (windows + halos at block level G, or whole subsystems)
+// ---------------------------------------------------------------------------
+template <int RPT>
+__global__ void __launch_bounds__(kMpThreads)
+mp_pass_kernel(MpPassArgs p)
+{
+    extern __shared__ float fsm[];
+    const int TRm = p.TRmax;
+    __shared__ unsigned s_max[2];
+
+    const int64_t blk = blockIdx.x;
+    const int64_t item = blk / p.nwin;
+    const int64_t w = blk - item * p.nwin;
+    const int64_t j = item / p.G;
+    const int64_t r = item - j * p.G;
+    if (p.fin[j]) return;
+    const int64_t nb = p.nb;
+    if (r >= nb) return;
+    const int64_t nr = (nb - 1 - r) / p.G + 1;
+    const int64_t wlo = w * (int64_t)p.L;
+    if (wlo >= nr) return;
+    const int64_t whi = min(wlo + (int64_t)p.L, nr);
+    const int64_t t0 = max(wlo - (int64_t)p.H, (int64_t)0);
+    const int64_t t1 = min(whi + (int64_t)p.H, nr);
+    const int TR = (int)(t1 - t0);
+    const int tid = threadIdx.x, bd = blockDim.x;
+    const int64_t g0 = j * nb + r;                 // block row of local t = 0
+    // a system whose couplings vanished in an earlier pass needs no more strides
+    const bool truncated = p.trunc_in && __uint_as_float(p.trunc_in[j]) < kTrunc;
+    const int K = truncated ? 0 : p.K;
+
+    for (int q = 0; q < RPT; q++) {
+        const int k = tid + q * bd;
+        if (k < TR) {
+            const int64_t gi = g0 + (t0 + k) * p.G;
+            float* s = fsm;
+            for (int u = 0; u < 8; u++) s[u * TRm + k] = p.srcLU[u][gi];
+            s[8 * TRm + k] = p.srcY[0][gi];
+            s[9 * TRm + k] = p.srcY[1][gi];
+        }
+    }
+    if (tid == 0) { s_max[0] = 0u; s_max[1] = 0u; }
+    __syncthreads();
+
+    int cur = 0;
+    for (int st = 0; st < K; st++) {
+        const int dl = 1 << st;
+        int64_t rlo, rhi;
+        if (p.final_step) { rlo = 0; rhi = nr; }
+        else {
+            const int64_t rem = (int64_t(1) << p.K) - (int64_t(2) << st);   // block halo = 2^K - 1
+            rlo = max(wlo - rem, (int64_t)0); rhi = min(whi + rem, nr);
+        }
+        const float* S = fsm + cur * 10 * TRm;
+        float* N = fsm + (cur ^ 1) * 10 * TRm;
+        float lmax = 0.0f;
+        for (int q = 0; q < RPT; q++) {
+            const int k = tid + q * bd;
+            const int64_t t = t0 + k;
+            if (k < TR && t >= rlo && t < rhi) {
+                const M2 Lk = {S[0 * TRm + k], S[1 * TRm + k], S[2 * TRm + k], S[3 * TRm + k]};
+                const M2 Uk = {S[4 * TRm + k], S[5 * TRm + k], S[6 * TRm + k], S[7 * TRm + k]};
+                float y0 = S[8 * TRm + k], y1 = S[9 * TRm + k];
+                M2 Dn = {1.0f, 0.0f, 0.0f, 1.0f}, Ln = {0, 0, 0, 0}, Un = {0, 0, 0, 0};
+                if (t - dl >= 0) {
+                    const int km = k - dl;
+                    const M2 Lm = {S[0 * TRm + km], S[1 * TRm + km], S[2 * TRm + km], S[3 * TRm + km]};
+                    const M2 Um = {S[4 * TRm + km], S[5 * TRm + km], S[6 * TRm + km], S[7 * TRm + km]};
+                    const float ym0 = S[8 * TRm + km], ym1 = S[9 * TRm + km];
+                    const M2 LU = mmul(Lk, Um), LL = mmul(Lk, Lm);
+                    Dn = {Dn.m0 - LU.m0, Dn.m1 - LU.m1, Dn.m2 - LU.m2, Dn.m3 - LU.m3};
+                    Ln = {-LL.m0, -LL.m1, -LL.m2, -LL.m3};
+                    y0 = fmaf(-Lk.m0, ym0, fmaf(-Lk.m1, ym1, y0));
+                    y1 = fmaf(-Lk.m2, ym0, fmaf(-Lk.m3, ym1, y1));
+                }
+                if (t + dl <= nr - 1) {
+                    const int kp = k + dl;
+                    const M2 Lp = {S[0 * TRm + kp], S[1 * TRm + kp], S[2 * TRm + kp], S[3 * TRm + kp]};
+                    const M2 Up = {S[4 * TRm + kp], S[5 * TRm + kp], S[6 * TRm + kp], S[7 * TRm + kp]};
+                    const float yp0 = S[8 * TRm + kp], yp1 = S[9 * TRm + kp];
+                    const M2 UL = mmul(Uk, Lp), UU = mmul(Uk, Up);
+                    Dn = {Dn.m0 - UL.m0, Dn.m1 - UL.m1, Dn.m2 - UL.m2, Dn.m3 - UL.m3};
+                    Un = {-UU.m0, -UU.m1, -UU.m2, -UU.m3};
+                    y0 = fmaf(-Uk.m0, yp0, fmaf(-Uk.m1, yp1, y0));
+                    y1 = fmaf(-Uk.m2, yp0, fmaf(-Uk.m3, yp1, y1));
+                }
+                const M2 Mi = minv(Dn);
+                const M2 L2 = mmul(Mi, Ln), U2 = mmul(Mi, Un);
+                N[0 * TRm + k] = L2.m0; N[1 * TRm + k] = L2.m1; N[2 * TRm + k] = L2.m2; N[3 * TRm + k] = L2.m3;
+                N[4 * TRm + k] = U2.m0; N[5 * TRm + k] = U2.m1; N[6 * TRm + k] = U2.m2; N[7 * TRm + k] = U2.m3;
+                N[8 * TRm + k] = fmaf(Mi.m0, y0, Mi.m1 * y1);
+                N[9 * TRm + k] = fmaf(Mi.m2, y0, Mi.m3 * y1);
+                lmax = fmaxf(lmax, fmaxf(fmaxf(fmaxf(fabsf(L2.m0), fabsf(L2.m1)), fmaxf(fabsf(L2.m2), fabsf(L2.m3))),
+                                         fmaxf(fmaxf(fabsf(U2.m0), fabsf(U2.m1)), fmaxf(fabsf(U2.m2), fabsf(U2.m3)))));
+            }
+        }
+        cur ^= 1;
+        if (p.final_step) {
+            // truncation test over the whole subsystem (one barrier per stride)
+            lmax = warp_max(lmax);
+            if ((tid & 31) == 0) atomicMax(&s_max[st & 1], __float_as_uint(lmax));
+            __syncthreads();
+            const float smax = __uint_as_float(s_max[st & 1]);
+            if (tid == 0) s_max[(st + 1) & 1] = 0u;
+            if (!(smax >= kTrunc)) break;                    // (nan also stops: the refinement will report it)
+            __syncthreads();
+        } else {
+            __syncthreads();
+        }
+    }
+
+    const float* S = fsm + cur * 10 * TRm;
+    if (p.final_step) {
+        // X = Y: write the correction rows and the system's |dx| maximum
+        float lmax = 0.0f;
+        for (int q = 0; q < RPT; q++) {
+            const int k = tid + q * bd;
+            if (k < TR) {
+                const int64_t kb = r + k * p.G;                 // block row within the system
+                const int64_t i0 = 2 * kb;
+                const float x0 = S[8 * TRm + k], x1 = S[9 * TRm + k];
+                p.dx[j * p.n + i0] = x0;
+                lmax = fmaxf(lmax, fabsf(x0));
+                if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = x1; lmax = fmaxf(lmax, fabsf(x1)); }
+            }
+        }
+        lmax = warp_max(lmax);
+        if ((tid & 31) == 0) atomic_max_pos(&p.ndx[(int64_t)p.sweep * p.m + j], lmax);
+    } else {
+        float lmax = 0.0f;
+        for (int q = 0; q < RPT; q++) {
+            const int k = tid + q * bd;
+            const int64_t t = t0 + k;
+            if (k < TR && t >= wlo && t < whi) {
+                const int64_t gi = g0 + t * p.G;
+                for (int u = 0; u < 8; u++) {
+                    const float v = S[u * TRm + k];
+                    p.dstLU[u][gi] = v;
+                    lmax = fmaxf(lmax, fabsf(v));
+                }
+                p.dstY[0][gi] = S[8 * TRm + k];
+                p.dstY[1][gi] = S[9 * TRm + k];
+            }
+        }
+        lmax = warp_max(lmax);
+        if ((tid & 31) == 0 && p.trunc_out) atomic_max_pos(&p.trunc_out[j], lmax);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// refinement: x += dx (FP64), decide, and r = y - A x for the next sweep
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kMpThreads)
+mp_update_kernel(MpArgs p)
+{
+    __shared__ double sx[kMpTile + 4];
+    __shared__ float s_red[kMpThreads / 32];
+    const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
+    const int64_t j = blockIdx.x / tiles;
+    const int64_t tile = blockIdx.x - j * tiles;
+    const int s = p.sweep;
+    // finished in an earlier sweep?  (fin is written by this kernel's tile-0 CTA
+    // for the current sweep; the other tiles of the system must still run)
+    const int f = p.fin[j];
+    if (f != 0 && f <= s) return;
+    const int tid = threadIdx.x;
+    const int64_t n = p.n;
+
+    // per-system decision from the norms the previous kernels left behind
+    const float nd = __uint_as_float(p.ndx[(int64_t)s * p.m + j]);
+    bool done = false;
+    float est = 0.0f;
+    if (s >= 1) {
+        const float ndp = __uint_as_float(p.ndx[(int64_t)(s - 1) * p.m + j]);
+        const float nxp = __uint_as_float(p.nx[(int64_t)(s - 1) * p.m + j]);
+        if (nd == 0.0f) { done = true; est = 0.0f; }
+        else if (ndp > 0.0f) {
+            // remaining error after this correction ~ sum_k rho^k |dx| = rho/(1-rho) |dx|;
+            // a factor 2 covers the drift of rho between sweeps
+            const float rho = nd / ndp;
+            est = rho < 0.5f ? 2.0f * rho / (1.0f - rho) * nd / fmaxf(nxp, FLT_MIN) : 1.0f;
+            done = rho < 0.5f && est <= p.tol;
+        }
+    }
+    const bool last = done || s == p.max_sweeps - 1;
+    const bool to_user = last && !p.keep_x;
+
+    // x_new on rows [t0-2, t0+TILE+2) (the halo rows are recomputed bit-identically by neighbours)
+    const int64_t t0 = tile * kMpTile;
+    const int64_t t1 = min(t0 + kMpTile, n);
+    const int64_t h0 = max(t0 - 2, (int64_t)0), h1 = min(t1 + 2, n);
+    for (int64_t i = h0 + tid; i < h1; i += blockDim.x) {
+        const double dxi = f2d(p.dx[j * n + i]);
+        sx[i - t0 + 2] = s == 0 ? dxi : __dadd_rn(p.X[j * n + i], dxi);
+    }
+    __syncthreads();
+
+    const int64_t ybase = j * p.ss;
+    float xmax = 0.0f;
+    for (int64_t i = t0 + tid; i < t1; i += blockDim.x) {
+        const double xi = sx[i - t0 + 2];
+        if (to_user) p.y[ybase + i * p.rs] = xi;
+        else p.X[j * n + i] = xi;
+        xmax = fmaxf(xmax, fabsf(d2f_scaled(xi, 0)));     // |x| in FP32: it only feeds the estimate
+    }
+    xmax = warp_max(xmax);
+    if ((tid & 31) == 0) s_red[tid >> 5] = xmax;
+    __syncthreads();
+    if (tid == 0) {
+        float v = 0.0f;
+        for (int w = 0; w < (int)(blockDim.x / 32); w++) v = fmaxf(v, s_red[w]);
+        atomic_max_pos(&p.nx[(int64_t)s * p.m + j], v);
+        if (tile == 0 && last) {
+            p.est[j] = est;
+            p.status[j] = done ? 1 : 2;      // 2: stopped at max_sweeps
+            p.fin[j] = s + 1;
+        }
+    }
+    if (last) return;
+
+    // residual r = y - A x (FP64, FMA chain), row-scaled to FP32 and normalised
+    // by the block's diagonal inverse -> right-hand side of the next FP32 solve
+    const int64_t nb = (n + 1) / 2;
+    const int64_t T = p.m * nb;
+    for (int64_t kb = t0 / 2 + tid; 2 * kb < t1; kb += blockDim.x) {
+        const BlockRow B = load_block(p.a, p.b, p.c, p.d, p.e, ybase, p.rs, 2 * kb, n);
+        float rf[2] = {0.0f, 0.0f};
+        for (int h = 0; h < 2; h++) {
+            const int64_t i = 2 * kb + h;
+            if (i >= n) break;
+            const int64_t g = ybase + i * p.rs;
+            const int li = (int)(i - t0 + 2);
+            double r = p.y[g];
+            r = fma(-p.c[g], sx[li], r);
+            if (i >= 2) r = fma(-p.a[g], sx[li - 2], r);
+            if (i >= 1) r = fma(-p.b[g], sx[li - 1], r);
+            if (i + 1 < n) r = fma(-p.d[g], sx[li + 1], r);
+            if (i + 2 < n) r = fma(-p.e[g], sx[li + 2], r);
+            rf[h] = d2f_scaled(r, h == 0 ? B.sh0 : B.sh1);
+        }
+        const M2 Mi = minv(B.D);
+        const int64_t q = j * nb + kb;
+        p.R[q] = fmaf(Mi.m0, rf[0], Mi.m1 * rf[1]);
+        p.R[T + q] = fmaf(Mi.m2, rf[0], Mi.m3 * rf[1]);
+    }
+}
+
+// r = y - A x (FP64 FMA chain).  Bands and y use the caller's layout (ss, rs);
+// x and r use (xss, xrs).
+__global__ void __launch_bounds__(kMpThreads)
+residual_kernel(const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
+                const double* __restrict__ d, const double* __restrict__ e, const double* __restrict__ y,
+                const double* __restrict__ x, double* __restrict__ r, int64_t m, int64_t n, int64_t ss, int64_t rs,
+                int64_t xss, int64_t xrs)
+{
+    const int64_t total = m * n;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        int64_t j, i;
+        if (rs == 1) { j = q / n; i = q - j * n; } else { i = q / m; j = q - i * m; }
+        const int64_t g = j * ss + i * rs;
+        const int64_t gx = j * xss + i * xrs;
+        double v = y[g];
+        v = fma(-c[g], x[gx], v);
+        if (i >= 2) v = fma(-a[g], x[gx - 2 * xrs], v);
+        if (i >= 1) v = fma(-b[g], x[gx - xrs], v);
+        if (i + 1 < n) v = fma(-d[g], x[gx + xrs], v);
+        if (i + 2 < n) v = fma(-e[g], x[gx + 2 * xrs], v);
+        r[gx] = v;
+    }
+}
+
+// x (workspace, contiguous) -> y (caller layout)
+__global__ void copy_out_kernel(const double* __restrict__ X, double* __restrict__ y, int64_t m, int64_t n,
+                                int64_t ss, int64_t rs)
+{
+    const int64_t total = m * n;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = q / n, i = q - j * n;
+        y[j * ss + i * rs] = X[q];
+    }
+}
+
+// Per system: max |r_i|, max_i sum_k |A_ik| and max |x_i| (float bit patterns).
+// X and r are contiguous; the bands use the caller's layout.
+__global__ void __launch_bounds__(kMpThreads)
+resid_norm_kernel(const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
+                  const double* __restrict__ d, const double* __restrict__ e,
+                  const double* __restrict__ X, const double* __restrict__ r, int64_t m, int64_t n,
+                  int64_t ss, int64_t rs, unsigned* __restrict__ rn, unsigned* __restrict__ an,
+                  unsigned* __restrict__ xn)
+{
+    const int64_t tiles = (n + 1023) / 1024;
+    const int64_t j = blockIdx.x / tiles, tile = blockIdx.x - j * tiles;
+    float rm = 0.0f, am = 0.0f, xm = 0.0f;
+    const int64_t iend = min((tile + 1) * 1024, n);
+    for (int64_t i = tile * 1024 + threadIdx.x; i < iend; i += blockDim.x) {
+        const int64_t g = j * ss + i * rs;
+        double rowsum = fabs(c[g]);
+        if (i >= 2) rowsum += fabs(a[g]);
+        if (i >= 1) rowsum += fabs(b[g]);
+        if (i + 1 < n) rowsum += fabs(d[g]);
+        if (i + 2 < n) rowsum += fabs(e[g]);
+        rm = fmaxf(rm, (float)fabs(r[j * n + i]));
+        am = fmaxf(am, (float)rowsum);
+        xm = fmaxf(xm, (float)fabs(X[j * n + i]));
+    }
+    rm = warp_max(rm); am = warp_max(am); xm = warp_max(xm);
+    if ((threadIdx.x & 31) == 0) {
+        atomic_max_pos(&rn[j], rm); atomic_max_pos(&an[j], am); atomic_max_pos(&xn[j], xm);
+    }
+}
+
+template <int RPT>
+cudaError_t launch_mp_pass_rpt(const MpPassArgs& p, int threads, int64_t blocks, cudaStream_t s)
+{
+    const size_t smem = (size_t)20 * p.TRmax * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(mp_pass_kernel<RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(20 * kMpMaxRows * sizeof(float)));
+    if (e != cudaSuccess) return e;
+    mp_pass_kernel<RPT><<<(unsigned)blocks, threads, smem, s>>>(p);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_mp_prep(const MpArgs& p, cudaStream_t s)
+{
+    const int64_t nb = (p.n + 1) / 2;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((p.m * nb + kMpThreads - 1) / kMpThreads, 152 * 16));
+    mp_prep_kernel<<<(unsigned)blocks, kMpThreads, 0, s>>>(p);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s)
+{
+    if (p.TRmax > kMpMaxRows) return cudaErrorInvalidValue;
+    int threads = kMpThreads;
+    if (p.TRmax < threads) threads = std::max(32, (p.TRmax + 31) / 32 * 32);
+    const int rpt = (p.TRmax + threads - 1) / threads;
+    const int64_t blocks = p.m * p.G * p.nwin;
+    if (blocks <= 0) return cudaSuccess;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    if (rpt <= 1) return launch_mp_pass_rpt<1>(p, threads, blocks, s);
+    if (rpt <= 2) return launch_mp_pass_rpt<2>(p, threads, blocks, s);
+    if (rpt <= 4) return launch_mp_pass_rpt<4>(p, threads, blocks, s);
+    if (rpt <= 8) return launch_mp_pass_rpt<8>(p, threads, blocks, s);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_mp_update(const MpArgs& p, cudaStream_t s)
+{
+    const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
+    const int64_t blocks = p.m * tiles;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    mp_update_kernel<<<(unsigned)blocks, kMpThreads, 0, s>>>(p);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_residual(const double* a, const double* b, const double* c, const double* d, const double* e,
+                            const double* y, const double* x, double* r, int64_t m, int64_t n, int64_t ss,
+                            int64_t rs, int64_t xss, int64_t xrs, cudaStream_t s)
+{
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((m * n + kMpThreads - 1) / kMpThreads, 152 * 16));
+    residual_kernel<<<(unsigned)blocks, kMpThreads, 0, s>>>(a, b, c, d, e, y, x, r, m, n, ss, rs, xss, xrs);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_copy_out(const double* X, double* y, int64_t m, int64_t n, int64_t ss, int64_t rs, cudaStream_t s)
+{
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((m * n + kMpThreads - 1) / kMpThreads, 152 * 16));
+    copy_out_kernel<<<(unsigned)blocks, kMpThreads, 0, s>>>(X, y, m, n, ss, rs);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resid_norm(const double* a, const double* b, const double* c, const double* d, const double* e,
+                              const double* X, const double* r, int64_t m, int64_t n, int64_t ss,
+                              int64_t rs, unsigned* rn, unsigned* an, unsigned* xn, cudaStream_t s)
+{
+    const int64_t blocks = m * ((n + 1023) / 1024);
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    resid_norm_kernel<<<(unsigned)blocks, kMpThreads, 0, s>>>(a, b, c, d, e, X, r, m, n, ss, rs, rn, an, xn);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace pcrp

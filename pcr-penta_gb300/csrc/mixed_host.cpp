@@ -1,0 +1,253 @@
+// mixed_host.cpp -- host side of the mixed-precision solver: workspace
+// layout, the FP32 pass plan and the refinement sweep loop.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "mixed_internal.h"
+#include "pcrp_internal.h"
+#include "tuned_params.h"
+
+namespace pcrp {
+
+pcrp_status get_workspace(const pcrp_opts* o, size_t bytes, cudaStream_t s, void** out);
+
+namespace {
+
+int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+struct MpPlan {
+    int cap;        // block rows solved whole in shared memory
+    int fuse;       // strides per global pass
+    int s1;         // global strides in total
+    int npass;
+};
+
+MpPlan mp_plan(int64_t nb, const pcrp_opts* o)
+{
+    static const int64_t table[][3] = PCRP_TUNED_MP_TABLE;
+    const int rows = (int)(sizeof(table) / sizeof(table[0]));
+    int t = 0;
+    while (t + 1 < rows && 2 * nb > table[t][0]) t++;
+    MpPlan p{(int)table[t][1], (int)table[t][2], 0, 0};
+    if (o && o->size >= sizeof(pcrp_opts)) {
+        if (o->smem_rows > 0) p.cap = std::max(1, o->smem_rows / 2);
+        if (o->fuse_strides > 0) p.fuse = o->fuse_strides;
+    }
+    p.cap = std::min(std::max(p.cap, 1), kMpMaxRows);
+    p.fuse = std::min(std::max(p.fuse, 1), 9);
+    while (cdiv(nb, int64_t(1) << p.s1) > p.cap) p.s1++;
+    p.npass = (int)cdiv(p.s1, p.fuse);
+    return p;
+}
+
+struct MpLayout {
+    size_t S0, R, P0, P1, dx, X, ndx, nx, fin, status, est, trunc, rbuf, rn, total;
+};
+
+MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool info)
+{
+    const int64_t nb = (n + 1) / 2, T = m * nb;
+    MpLayout L{};
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
+    L.S0 = take(8 * T * sizeof(float));
+    L.R = take(2 * T * sizeof(float));
+    L.P0 = pl.s1 > 0 ? take(10 * T * sizeof(float)) : 0;
+    L.P1 = pl.npass > 1 ? take(10 * T * sizeof(float)) : 0;
+    L.dx = take((size_t)m * n * sizeof(float));
+    L.X = take((size_t)m * n * sizeof(double));
+    L.ndx = take((size_t)(max_sweeps + 1) * m * sizeof(unsigned));
+    L.nx = take((size_t)(max_sweeps + 1) * m * sizeof(unsigned));
+    L.fin = take(m * sizeof(int));
+    L.status = take(m * sizeof(int));
+    L.est = take(m * sizeof(float));
+    L.trunc = take((size_t)kMpMaxPasses * m * sizeof(unsigned));
+    L.rbuf = info ? take((size_t)m * n * sizeof(double)) : 0;
+    L.rn = info ? take(3 * m * sizeof(unsigned)) : 0;
+    L.total = off;
+    return L;
+}
+
+bool valid_layout(int32_t l) { return l == PCRP_LAYOUT_CONTIGUOUS || l == PCRP_LAYOUT_INTERLEAVED; }
+
+}  // namespace
+
+size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_sweeps, bool info)
+{
+    if (m <= 0 || n <= 0) return 0;
+    const MpPlan pl = mp_plan((n + 1) / 2, o);
+    return mp_layout(m, n, max_sweeps, pl, info).total;
+}
+
+// Enqueues prep + max_sweeps refinement sweeps of a uniform batch on `st`
+// using the workspace `ws` (mixed_workspace_bytes(m, n, opts, max_sweeps, keep_x)
+// bytes).  The bands and y use addressing (ss, rs).  Fills *out with the
+// kernel arguments (per-system status arrays live in the workspace).
+pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, const double* d, const double* e,
+                          double* y, int64_t m, int64_t n, int64_t ss, int64_t rs, double tol, int max_sweeps,
+                          const pcrp_opts* opts, bool keep_x, void* ws, cudaStream_t st, MpArgs* out)
+{
+    const char* who = "pcrp_solve_mixed";
+    const int64_t nb = (n + 1) / 2, T = m * nb;
+    const MpPlan pl = mp_plan(nb, opts);
+    if (pl.npass > kMpMaxPasses) return set_error(PCRP_EINVAL, "%s: n too large for the pass plan", who);
+    const MpLayout WL = mp_layout(m, n, max_sweeps, pl, keep_x);
+    char* base = static_cast<char*>(ws);
+    auto F = [&](size_t off) { return reinterpret_cast<float*>(base + off); };
+    auto U = [&](size_t off) { return reinterpret_cast<unsigned*>(base + off); };
+
+    MpArgs A{};
+    A.a = a; A.b = b; A.c = c; A.d = d; A.e = e; A.y = y;
+    A.m = m; A.n = n; A.ss = ss; A.rs = rs;
+    A.S0 = F(WL.S0); A.R = F(WL.R); A.dx = F(WL.dx);
+    A.X = reinterpret_cast<double*>(base + WL.X);
+    A.ndx = U(WL.ndx); A.nx = U(WL.nx);
+    A.fin = reinterpret_cast<int*>(base + WL.fin);
+    A.status = reinterpret_cast<int*>(base + WL.status);
+    A.est = F(WL.est); A.trunc = U(WL.trunc);
+    A.max_sweeps = max_sweeps; A.tol = (float)tol; A.keep_x = keep_x;
+
+    cudaError_t ce = launch_mp_prep(A, st);
+    if (ce != cudaSuccess) return cuda_error(ce, "mixed prep launch");
+
+    float* P[2] = {pl.s1 > 0 ? F(WL.P0) : nullptr, pl.npass > 1 ? F(WL.P1) : nullptr};
+    for (int s = 0; s < max_sweeps; s++) {
+        // FP32 block-PCR solve of the normalised system with rhs R
+        MpPassArgs p{};
+        for (int u = 0; u < 8; u++) p.srcLU[u] = A.S0 + u * T;
+        p.srcY[0] = A.R; p.srcY[1] = A.R + T;
+        p.dx = A.dx; p.fin = A.fin; p.ndx = A.ndx;
+        p.m = m; p.n = n; p.nb = nb; p.G = 1; p.sweep = s;
+        int done = 0, pass = 0;
+        while (done < pl.s1) {
+            const int K = std::min(pl.fuse, pl.s1 - done);
+            const int H = (1 << K) - 1;
+            int Lw = std::max(1, pl.cap - 2 * H);
+            const int64_t nrmax = cdiv(nb, p.G);
+            float* D = P[pass & 1];
+            for (int u = 0; u < 8; u++) p.dstLU[u] = D + u * T;
+            p.dstY[0] = D + 8 * T; p.dstY[1] = D + 9 * T;
+            p.K = K; p.H = H; p.L = Lw; p.final_step = 0;
+            p.nwin = cdiv(nrmax, Lw);
+            p.TRmax = (int)std::min<int64_t>(Lw + 2 * H, nrmax);
+            p.trunc_in = pass > 0 ? A.trunc + (pass - 1) * m : nullptr;
+            p.trunc_out = A.trunc + pass * m;
+            ce = launch_mp_pass(p, st);
+            if (ce != cudaSuccess) return cuda_error(ce, "mixed global pass launch");
+            for (int u = 0; u < 8; u++) p.srcLU[u] = D + u * T;
+            p.srcY[0] = D + 8 * T; p.srcY[1] = D + 9 * T;
+            p.G <<= K; done += K; pass++;
+        }
+        const int64_t nrmax = cdiv(nb, p.G);
+        int Kf = 0;
+        while ((int64_t(1) << Kf) < nrmax) Kf++;
+        p.K = Kf; p.H = 0; p.L = (int)nrmax; p.final_step = 1; p.nwin = 1; p.TRmax = (int)nrmax;
+        p.trunc_in = pass > 0 ? A.trunc + (pass - 1) * m : nullptr;
+        p.trunc_out = nullptr;
+        ce = launch_mp_pass(p, st);
+        if (ce != cudaSuccess) return cuda_error(ce, "mixed shared-memory pass launch");
+        // FP64 update, stopping decision, next residual
+        A.sweep = s;
+        ce = launch_mp_update(A, st);
+        if (ce != cudaSuccess) return cuda_error(ce, "mixed refinement launch");
+    }
+    if (out) *out = A;
+    return PCRP_OK;
+}
+
+}  // namespace pcrp
+
+using namespace pcrp;
+
+extern "C" pcrp_status pcrp_solve_mixed(const double* a, const double* b, const double* c, const double* d,
+                                        const double* e, double* y, int64_t m, int64_t n, int32_t layout,
+                                        double tol, int32_t max_sweeps, const pcrp_opts* opts, pcrp_stream stream,
+                                        pcrp_mixed_info* info)
+{
+    const char* who = "pcrp_solve_mixed";
+    if (m < 0 || n < 0) return set_error(PCRP_EINVAL, "%s: negative size", who);
+    if (!valid_layout(layout)) return set_error(PCRP_EINVAL, "%s: bad layout %d", who, layout);
+    if (info) std::memset(info, 0, sizeof *info);
+    if (m == 0 || n == 0) { if (info) info->converged = 1; return PCRP_OK; }
+    if (!a || !b || !c || !d || !e || !y) return set_error(PCRP_EINVAL, "%s: null array", who);
+    if (n > (int64_t(1) << 31) || m > (int64_t(1) << 24))
+        return set_error(PCRP_EINVAL, "%s: size out of range (m <= 2^24, n <= 2^31)", who);
+    if (!(tol > 0.0)) tol = 1e-12;
+    if (max_sweeps <= 0) max_sweeps = 8;
+    if (max_sweeps > 64) max_sweeps = 64;
+    cudaStream_t st = (cudaStream_t)stream;
+
+    const int64_t nb = (n + 1) / 2;
+    const MpPlan pl = mp_plan(nb, opts);
+    if (pl.npass > kMpMaxPasses) return set_error(PCRP_EINVAL, "%s: n too large for the pass plan", who);
+    const MpLayout WL = mp_layout(m, n, max_sweeps, pl, info != nullptr);
+    void* ws = nullptr;
+    pcrp_status rc = get_workspace(opts, WL.total, st, &ws);
+    if (rc != PCRP_OK) return rc;
+    char* base = static_cast<char*>(ws);
+    auto U = [&](size_t off) { return reinterpret_cast<unsigned*>(base + off); };
+    MpArgs A{};
+    rc = mixed_enqueue(a, b, c, d, e, y, m, n, layout == PCRP_LAYOUT_CONTIGUOUS ? n : 1,
+                       layout == PCRP_LAYOUT_CONTIGUOUS ? 1 : m, tol, max_sweeps, opts, info != nullptr, ws, st, &A);
+    if (rc != PCRP_OK) return rc;
+    cudaError_t ce;
+
+    if (!info) return PCRP_OK;
+
+    // report: y still holds the rhs (the iterate was kept in X); final
+    // residual r = y - A X, its norms, then X -> y
+    double* rb = reinterpret_cast<double*>(base + WL.rbuf);
+    unsigned* rn = U(WL.rn);
+    ce = cudaMemsetAsync(rn, 0, 3 * m * sizeof(unsigned), st);
+    if (ce != cudaSuccess) return cuda_error(ce, "cudaMemsetAsync");
+    ce = launch_residual(a, b, c, d, e, y, A.X, rb, m, n, A.ss, A.rs, n, 1, st);
+    if (ce == cudaSuccess) ce = launch_resid_norm(a, b, c, d, e, A.X, rb, m, n, A.ss, A.rs, rn, rn + m, rn + 2 * m, st);
+    if (ce == cudaSuccess) ce = launch_copy_out(A.X, y, m, n, A.ss, A.rs, st);
+    if (ce != cudaSuccess) return cuda_error(ce, "mixed report launch");
+    std::vector<unsigned> norms(3 * m);
+    ce = cudaMemcpyAsync(norms.data(), rn, 3 * m * sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (ce != cudaSuccess) return cuda_error(ce, "mixed report copy");
+    std::vector<int> conv(m), sw(m);
+    std::vector<float> est(m);
+    ce = cudaMemcpyAsync(conv.data(), A.status, m * sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(sw.data(), A.fin, m * sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(est.data(), A.est, m * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return cuda_error(ce, "mixed report");
+    int all = 1, maxsw = 0;
+    float maxest = 0.0f;
+    for (int64_t j = 0; j < m; j++) {
+        all &= conv[j] == 1;
+        maxsw = std::max(maxsw, sw[j]);
+        maxest = std::max(maxest, est[j]);
+    }
+    info->sweeps = maxsw;
+    info->converged = all;
+    info->fwd_err_est = maxest;
+    double worst = 0.0;
+    for (int64_t j = 0; j < m; j++) {
+        float rj, aj, xj;
+        std::memcpy(&rj, &norms[j], 4); std::memcpy(&aj, &norms[m + j], 4); std::memcpy(&xj, &norms[2 * m + j], 4);
+        const double den = (double)aj * (double)xj;
+        const double v = den > 0.0 ? rj / den : (rj > 0.0f ? 1.0 : 0.0);
+        worst = std::max(worst, v);
+    }
+    info->resid = worst;
+    if (!all) return set_error(PCRP_ENOCONV, "%s: not every system reached tol=%g in %d sweeps", who, tol, max_sweeps);
+    return PCRP_OK;
+}
+
+extern "C" pcrp_status pcrp_residual_f64(const double* a, const double* b, const double* c, const double* d,
+                                         const double* e, const double* y, const double* x, double* r,
+                                         int64_t m, int64_t n, int32_t layout, pcrp_stream stream)
+{
+    if (m < 0 || n < 0) return set_error(PCRP_EINVAL, "pcrp_residual_f64: negative size");
+    if (!valid_layout(layout)) return set_error(PCRP_EINVAL, "pcrp_residual_f64: bad layout %d", layout);
+    if (m == 0 || n == 0) return PCRP_OK;
+    if (!a || !b || !c || !d || !e || !y || !x || !r) return set_error(PCRP_EINVAL, "pcrp_residual_f64: null array");
+    if (r == x) return set_error(PCRP_EINVAL, "pcrp_residual_f64: r may not alias x");
+    const int64_t ss = layout == PCRP_LAYOUT_CONTIGUOUS ? n : 1, rs = layout == PCRP_LAYOUT_CONTIGUOUS ? 1 : m;
+    return cuda_error(launch_residual(a, b, c, d, e, y, x, r, m, n, ss, rs, ss, rs, (cudaStream_t)stream),
+                      "pcrp_residual_f64 launch");
+}

@@ -1,0 +1,57 @@
+// mixed_internal.h -- argument blocks and launchers of the mixed-precision solver.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pcrp {
+
+constexpr int kMpTile = 1024;      // rows per CTA of the refinement kernel (even)
+constexpr int kMpMaxRows = 2048;   // block rows per CTA of the FP32 PCR kernel (20 floats each)
+constexpr int kMpMaxPasses = 24;   // global FP32 passes per solve
+
+// Whole-batch arguments (prep and refinement kernels).
+struct MpArgs {
+    const double *a, *b, *c, *d, *e;   // caller bands, layout (ss, rs)
+    double* y;                          // caller rhs in, solution out
+    int64_t m, n, ss, rs;
+    float* S0;                          // level-0 normalised L,U: 8 arrays of m*nb
+    float* R;                           // normalised rhs Y: 2 arrays of m*nb
+    float* dx;                          // FP32 correction, m*n (contiguous)
+    double* X;                          // FP64 iterate, m*n (contiguous)
+    unsigned* ndx;                      // [(max_sweeps+1) x m] max |dx| per sweep (float bits)
+    unsigned* nx;                       // [(max_sweeps+1) x m] max |x| per sweep
+    int* fin;                           // per system: 0 running, else the sweep it finished in, plus 1
+    int* status;                        // per system: 1 converged, 2 stopped at max_sweeps
+    float* est;                         // per system: estimated relative forward error
+    unsigned* trunc;                    // [kMpMaxPasses x m] max |L|,|U| after each global pass
+    int sweep, max_sweeps, keep_x;
+    float tol;
+};
+
+// One FP32 block-PCR pass.
+struct MpPassArgs {
+    const float* srcLU[8];
+    const float* srcY[2];
+    float* dstLU[8];
+    float* dstY[2];
+    float* dx;
+    const int* fin;                     // systems with fin != 0 are finished: skip them
+    unsigned* ndx;                      // final pass: max |dx| of this sweep
+    const unsigned* trunc_in;           // previous pass's max |L|,|U| (or null)
+    unsigned* trunc_out;                // this pass's max |L|,|U| (non-final)
+    int64_t m, n, nb, G, nwin;
+    int K, final_step, L, H, TRmax, sweep;
+};
+
+cudaError_t launch_mp_prep(const MpArgs& p, cudaStream_t s);
+cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s);
+cudaError_t launch_mp_update(const MpArgs& p, cudaStream_t s);
+cudaError_t launch_residual(const double* a, const double* b, const double* c, const double* d, const double* e,
+                            const double* y, const double* x, double* r, int64_t m, int64_t n, int64_t ss,
+                            int64_t rs, int64_t xss, int64_t xrs, cudaStream_t s);
+cudaError_t launch_copy_out(const double* X, double* y, int64_t m, int64_t n, int64_t ss, int64_t rs, cudaStream_t s);
+cudaError_t launch_resid_norm(const double* a, const double* b, const double* c, const double* d, const double* e,
+                              const double* X, const double* r, int64_t m, int64_t n, int64_t ss,
+                              int64_t rs, unsigned* rn, unsigned* an, unsigned* xn, cudaStream_t s);
+
+}  // namespace pcrp

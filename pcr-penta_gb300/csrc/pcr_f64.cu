@@ -34,210 +34,24 @@
 // part, so this kernel is bounded by the FP64 pipe, not HBM; the design goal
 // is to keep that pipe busy (several CTAs per SM, 4 rows per thread for ILP)
 // and to spend no FP64 operation beyond the reference's own arithmetic.
-#include "pcrp_internal.h"
+#include "pcr_tile.cuh"
 
 namespace pcrp {
 namespace {
-
-__device__ __forceinline__ double mul(double x, double y) { return __dmul_rn(x, y); }
-__device__ __forceinline__ double add(double x, double y) { return __dadd_rn(x, y); }
-__device__ __forceinline__ double sub(double x, double y) { return __dsub_rn(x, y); }
-__device__ __forceinline__ double dvd(double x, double y) { return __ddiv_rn(x, y); }
-
-constexpr int kMaxThreads = 256;
-constexpr int kSmemArrays = 14;   // 6 state + 6 T coefficients + 2 T multipliers
 
 template <int RPT>
 __global__ void __launch_bounds__(kMaxThreads, 2)
 pcr_pass_kernel(const PcrPassArgs p)
 {
     extern __shared__ double smem[];
-    const int TRm = p.TRmax;
-    double* sa = smem;            double* sb = sa + TRm;  double* sc = sb + TRm;
-    double* sd = sc + TRm;        double* se = sd + TRm;  double* sy = se + TRm;
-    double* Ta = sy + TRm;        double* Tb = Ta + TRm;  double* Tc = Tb + TRm;
-    double* Td = Tc + TRm;        double* Te = Td + TRm;  double* Tk = Te + TRm;
-    double* T1 = Tk + TRm;        double* T2 = T1 + TRm;
-
     const int64_t blk  = blockIdx.x;
     const int64_t item = blk / p.nwin;
     const int64_t w    = blk - item * p.nwin;
     const int64_t j    = item / p.G;
     const int64_t r    = item - j * p.G;
-    const int64_t sbase = p.offsets ? p.offsets[j] : j * p.src_ss;
-    const int64_t dbase = p.offsets ? p.offsets[j] : j * p.dst_ss;
-    const int64_t nsys = p.offsets ? (p.offsets[j + 1] - p.offsets[j]) : p.n;
-    if (r >= nsys) return;
-    const int64_t nr  = (nsys - 1 - r) / p.G + 1;           // rows of subsystem r
-    const int64_t wlo = w * (int64_t)p.L;
-    if (wlo >= nr) return;
-    const int64_t whi = min(wlo + (int64_t)p.L, nr);
-    const int64_t t0  = max(wlo - (int64_t)p.H, (int64_t)0);
-    const int64_t t1  = min(whi + (int64_t)p.H, nr);
-    const int TR = (int)(t1 - t0);
-    const int tid = threadIdx.x, bd = blockDim.x;
-    const int64_t sstep = p.G * p.src_rs;                   // distance of local rows t, t+1
-    const int64_t dstep = p.G * p.dst_rs;
-    const int64_t soff = sbase + r * p.src_rs;              // local row 0
-    const int64_t doff = dbase + r * p.dst_rs;
-    const double* __restrict__ ga = p.src[A_] + soff;
-    const double* __restrict__ gb = p.src[B_] + soff;
-    const double* __restrict__ gc = p.src[C_] + soff;
-    const double* __restrict__ gd = p.src[D_] + soff;
-    const double* __restrict__ ge = p.src[E_] + soff;
-    const double* __restrict__ gy = p.src[Y_] + soff;
-
-    double al1p[RPT], al2p[RPT];
-#pragma unroll
-    for (int q = 0; q < RPT; q++) {
-        const int k = tid + q * bd;
-        al1p[q] = 0.0; al2p[q] = 0.0;
-        if (k < TR) {
-            const int64_t gi = (t0 + k) * sstep;
-            sa[k] = ga[gi]; sb[k] = gb[gi]; sc[k] = gc[gi];
-            sd[k] = gd[gi]; se[k] = ge[gi]; sy[k] = gy[gi];
-            if (p.src[AL1_]) {
-                al1p[q] = p.src[AL1_][soff + gi];
-                al2p[q] = p.src[AL2_][soff + gi];
-            }
-        }
-    }
-    __syncthreads();
-
-    for (int s = 0; s < p.K; s++) {
-        const int dl = 1 << s;
-        // rows this stride must produce: the window widened by the halo the
-        // remaining strides of the pass still consume (everything if final).
-        int64_t rlo, rhi;
-        if (p.final_step) { rlo = 0; rhi = nr; }
-        else {
-            const int64_t rem = 2 * ((int64_t(1) << p.K) - (int64_t(2) << s));
-            rlo = max(wlo - rem, (int64_t)0); rhi = min(whi + rem, nr);
-        }
-        const int64_t Tlo = max(rlo - dl, (int64_t)0), Thi = min(rhi + dl, nr);
-
-        // ---- phase A: T(m) = a1*row(m-d) + row(m) + a2*row(m+d) ----------
-#pragma unroll
-        for (int q = 0; q < RPT; q++) {
-            const int k = tid + q * bd;
-            const int64_t t = t0 + k;
-            if (k < TR && t >= Tlo && t < Thi) {
-                const bool hasL = t - dl >= 0, hasR = t + dl <= nr - 1;
-                if (hasL || hasR) {
-                    const double am = sa[k], bm = sb[k], cm = sc[k], dm = sd[k], em = se[k], ym = sy[k];
-                    double al1 = 0.0, al2 = 0.0;
-                    double aT, bT, cT, dT, eT, kT;
-                    if (hasL && hasR) {
-                        const double aL = sa[k - dl], bL = sb[k - dl], cL = sc[k - dl], dL = sd[k - dl],
-                                     eL = se[k - dl], yL = sy[k - dl];
-                        const double aR = sa[k + dl], bR = sb[k + dl], cR = sc[k + dl], dR = sd[k + dl],
-                                     eR = se[k + dl], yR = sy[k + dl];
-                        if (t - 2 * dl >= 0 && bL != 0.0) al1 = dvd(-am, bL);
-                        if (t + 2 * dl <= nr - 1 && dR != 0.0) al2 = dvd(-em, dR);
-                        aT = mul(al1, aL);
-                        bT = add(add(mul(al1, cL), bm), mul(al2, aR));
-                        cT = add(add(mul(al1, dL), cm), mul(al2, bR));
-                        dT = add(add(mul(al1, eL), dm), mul(al2, cR));
-                        eT = mul(al2, eR);
-                        kT = add(add(mul(al1, yL), ym), mul(al2, yR));
-                    } else if (hasR) {     // row m-d outside: kernel.cu:82-91
-                        const double aR = sa[k + dl], bR = sb[k + dl], cR = sc[k + dl], dR = sd[k + dl],
-                                     eR = se[k + dl], yR = sy[k + dl];
-                        (void)aR;
-                        if (t + 2 * dl <= nr - 1 && dR != 0.0) al2 = dvd(-em, dR);
-                        aT = 0.0; bT = 0.0;
-                        cT = add(cm, mul(al2, bR));
-                        dT = add(dm, mul(al2, cR));
-                        eT = mul(al2, eR);
-                        kT = add(ym, mul(al2, yR));
-                    } else {               // row m+d outside: kernel.cu:108-117
-                        const double aL = sa[k - dl], bL = sb[k - dl], cL = sc[k - dl], dL = sd[k - dl],
-                                     yL = sy[k - dl];
-                        if (t - 2 * dl >= 0 && bL != 0.0) al1 = dvd(-am, bL);
-                        aT = mul(al1, aL);
-                        bT = add(mul(al1, cL), bm);
-                        cT = add(mul(al1, dL), cm);
-                        dT = 0.0; eT = 0.0;
-                        kT = add(mul(al1, yL), ym);
-                        (void)em;
-                    }
-                    Ta[k] = aT; Tb[k] = bT; Tc[k] = cT; Td[k] = dT; Te[k] = eT; Tk[k] = kT;
-                    T1[k] = al1; T2[k] = al2;
-                }
-            }
-        }
-        __syncthreads();
-
-        // ---- phase B: new row = b/cT(i-d)*T(i-d) - row(i) + d/cT(i+d)*T(i+d)
-#pragma unroll
-        for (int q = 0; q < RPT; q++) {
-            const int k = tid + q * bd;
-            const int64_t t = t0 + k;
-            if (k < TR && t >= rlo && t < rhi) {
-                const bool hasL = t - dl >= 0, hasR = t + dl <= nr - 1;
-                const double ai = sa[k], bi = sb[k], ci = sc[k], di = sd[k], ei = se[k], yi = sy[k];
-                // multipliers last assigned before Reduction-III (kernel.cu:96-112)
-                const double a1pre = hasR ? T1[k + dl] : ((t - 2 * dl >= 0) ? T1[k - dl] : al1p[q]);
-                const double a2pre = (t + 2 * dl <= nr - 1) ? T2[k + dl] : (hasL ? T2[k - dl] : al2p[q]);
-                double a1 = 0.0, b1 = 0.0, c1 = 0.0, d1 = 0.0, k1 = 0.0, f1 = a1pre;
-                double b2 = 0.0, c2 = 0.0, d2 = 0.0, e2 = 0.0, k2 = 0.0, f2 = a2pre;
-                if (hasL) {                // kernel.cu:120-125
-                    const double cTL = Tc[k - dl];
-                    if (cTL != 0.0) f1 = dvd(bi, cTL);
-                    a1 = mul(f1, Ta[k - dl]); b1 = mul(f1, Tb[k - dl]); c1 = mul(f1, Td[k - dl]);
-                    d1 = mul(f1, Te[k - dl]); k1 = mul(f1, Tk[k - dl]);
-                }
-                if (hasR) {                // kernel.cu:127-132
-                    const double cTR = Tc[k + dl];
-                    if (cTR != 0.0) f2 = dvd(di, cTR);
-                    c2 = mul(f2, Tb[k + dl]); b2 = mul(f2, Ta[k + dl]); d2 = mul(f2, Td[k + dl]);
-                    e2 = mul(f2, Te[k + dl]); k2 = mul(f2, Tk[k + dl]);
-                }
-                // kernel.cu:138-140 (in place: phase B reads no other row's state)
-                sb[k] = add(sub(b1, ai), b2);
-                sc[k] = add(sub(c1, ci), c2);
-                sd[k] = add(sub(d1, ei), d2);
-                sy[k] = add(sub(k1, yi), k2);
-                sa[k] = a1;
-                se[k] = e2;
-                al1p[q] = f1; al2p[q] = f2;
-            }
-        }
-        __syncthreads();
-    }
-
-    if (p.final_step) {
-        // kernel.cu:145-153: pairs (i, i+delta) by Cramer's rule, singles x = y/c
-        const int64_t df = int64_t(1) << p.K;
-        double* __restrict__ gx = p.x + doff;
-#pragma unroll
-        for (int q = 0; q < RPT; q++) {
-            const int k = tid + q * bd;
-            if (k < TR) {
-                const int64_t t = k;       // whole subsystem: t0 == 0
-                if (t < nr - df) {
-                    const int kk = k + (int)df;
-                    const double deno = sub(mul(sc[k], sc[kk]), mul(sb[kk], sd[k]));
-                    gx[t * dstep] = dvd(sub(mul(sc[kk], sy[k]), mul(sd[k], sy[kk])), deno);
-                    gx[(t + df) * dstep] = dvd(sub(mul(sc[k], sy[kk]), mul(sb[kk], sy[k])), deno);
-                }
-                if (t >= nr - df && t < df) gx[t * dstep] = dvd(sy[k], sc[k]);
-            }
-        }
-    } else {
-#pragma unroll
-        for (int q = 0; q < RPT; q++) {
-            const int k = tid + q * bd;
-            const int64_t t = t0 + k;
-            if (k < TR && t >= wlo && t < whi) {
-                const int64_t gi = doff + t * dstep;
-                p.dst[A_][gi] = sa[k]; p.dst[B_][gi] = sb[k]; p.dst[C_][gi] = sc[k];
-                p.dst[D_][gi] = sd[k]; p.dst[E_][gi] = se[k]; p.dst[Y_][gi] = sy[k];
-                p.dst[AL1_][gi] = al1p[q]; p.dst[AL2_][gi] = al2p[q];
-            }
-        }
-    }
+    pcr_tile<RPT>(p, j, r, w, smem);
 }
+
 
 template <int RPT>
 cudaError_t launch_rpt(const PcrPassArgs& p, int threads, size_t smem, int64_t blocks, cudaStream_t s)

@@ -1,0 +1,370 @@
+// ragged.cu -- ragged batches (systems of uneven n) in one persistent kernel.
+//
+// Every system k (rows offsets[k] .. offsets[k+1]-1) is cut into work items
+// with the same plan pcrp_solve_f64 uses for a uniform batch: P_k global
+// levels of fused strides (items = residues x windows) and one finishing level
+// of whole subsystems (items = residues).  Systems of at most `cap` rows have
+// P_k = 0 and a single finishing item: they are "binned" to the shared-memory
+// path, the others to the global path.  The items of all systems form one
+// queue ordered by level, then by system; CTAs of a persistent grid claim them
+// with an atomic counter and run them with the same per-CTA code as the
+// uniform kernels (pcr_tile), so each system's result is bit-identical to
+// pcrp_solve_f64 on that system.
+//
+// A level-l item of system k reads what the level-(l-1) items of k wrote.
+// The producing CTA publishes with __threadfence + atomicAdd on a per
+// (level, system) counter; the consumer polls that counter.  Items are
+// claimed in queue order and every dependency precedes its dependent in the
+// queue, so the oldest unfinished item never waits and the queue drains.
+// Each wait is bounded (kSpinLimit polls, about 4 s); on expiry the item sets
+// an error flag, skips its work and the host reports PCRP_ETIMEOUT.  State
+// written by other CTAs during the launch is read through L2 only.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "pcr_tile.cuh"
+#include "tuned_params.h"
+
+namespace pcrp {
+
+pcrp_status get_workspace(const pcrp_opts* o, size_t bytes, cudaStream_t s, void** out);
+
+namespace {
+
+constexpr int kRgThreads = 256;
+constexpr int kRgRPT = 4;                  // rows per thread: capacity 1024 rows
+constexpr int kRgCap = kRgThreads * kRgRPT;
+constexpr int kMaxLevels = 24;             // global levels + finish
+constexpr long long kSpinLimit = 1LL << 24;
+constexpr long long kSpinLimitInjected = 1LL << 14;   // ~4 ms: the failure-detection test
+
+struct RgArgs {
+    const double* src[6];                  // caller bands + rhs
+    double* y;                             // solution out
+    double* buf[2][NSTATE];                // ping-pong pass state, laid out like the caller arrays
+    const int64_t* offsets;
+    int64_t nsys;
+    int cap, fuse, L;
+    int64_t* count;                        // [kMaxLevels][nsys] items per (level, system)
+    int64_t* start;                        // [kMaxLevels*nsys + 1] exclusive prefix, level-major
+    unsigned* done;                        // [kMaxLevels][nsys] finished items
+    unsigned long long* head;              // next item to claim
+    int* err;                              // 1: a wait gave up
+    int inject;                            // test hook: system 0 waits for an item that never comes
+};
+
+__host__ __device__ inline int64_t cdiv64(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Plan of one system: returns the number of global levels P and fills the
+// strides K, gather stride G (before the level) and windows of each level.
+__device__ inline int rg_plan(int64_t n, int cap, int fuse, int L0, int* K, int64_t* G, int64_t* nwin, int* H, int* Lw)
+{
+    const int ns = ref_strides(n);
+    int s1 = 0;
+    while (s1 < ns && cdiv64(n, int64_t(1) << s1) > cap) s1++;
+    int P = 0, done = 0;
+    int64_t g = 1;
+    while (done < s1) {
+        const int k = min(fuse, s1 - done);
+        const int h = 2 * ((1 << k) - 1);
+        int l = L0 > 0 ? L0 : cap;
+        if (l + 2 * h > cap) l = cap - 2 * h;
+        if (l < 1) l = 1;
+        K[P] = k; G[P] = g; H[P] = h; Lw[P] = l;
+        nwin[P] = cdiv64(cdiv64(n, g), l);
+        g <<= k; done += k; P++;
+    }
+    K[P] = ns - s1; G[P] = g; H[P] = 0; Lw[P] = (int)cdiv64(n, g); nwin[P] = 1;
+    return P;
+}
+
+__global__ void rg_plan_kernel(RgArgs a)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.nsys; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t n = a.offsets[k + 1] - a.offsets[k];
+        int K[kMaxLevels], H[kMaxLevels], Lw[kMaxLevels];
+        int64_t G[kMaxLevels], nwin[kMaxLevels];
+        int P = n > 0 ? rg_plan(n, a.cap, a.fuse, a.L, K, G, nwin, H, Lw) : -1;
+        for (int l = 0; l < kMaxLevels; l++) {
+            int64_t c = 0;
+            if (l < P) c = G[l] * nwin[l];
+            else if (l == P) c = min(G[P], n);          // one item per non-empty residue
+            a.count[(int64_t)l * a.nsys + k] = c;
+            a.done[(int64_t)l * a.nsys + k] = 0u;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) { *a.head = 0ull; *a.err = 0; }
+}
+
+// exclusive scan of count (level-major) into start; one CTA
+__global__ void rg_scan_kernel(RgArgs a)
+{
+    __shared__ int64_t part[1024];
+    const int64_t total = (int64_t)kMaxLevels * a.nsys;
+    const int64_t per = cdiv64(total, blockDim.x);
+    const int64_t b0 = threadIdx.x * per, b1 = min(b0 + per, total);
+    int64_t s = 0;
+    for (int64_t i = b0; i < b1; i++) s += a.count[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t acc = 0;
+        for (int t = 0; t < (int)blockDim.x; t++) { const int64_t v = part[t]; part[t] = acc; acc += v; }
+        a.start[total] = acc;
+    }
+    __syncthreads();
+    int64_t acc = part[threadIdx.x];
+    for (int64_t i = b0; i < b1; i++) { a.start[i] = acc; acc += a.count[i]; }
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__global__ void __launch_bounds__(kRgThreads, 2)
+rg_persistent_kernel(RgArgs a)
+{
+    extern __shared__ double smem[];
+    __shared__ long long s_item;
+    __shared__ int s_skip;
+    const int64_t total_slots = (int64_t)kMaxLevels * a.nsys;
+    const int64_t total = a.start[total_slots];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (long long)atomicAdd(a.head, 1ull);
+        __syncthreads();
+        const int64_t item = s_item;
+        if (item >= total) break;
+        // slot = last (level, system) whose start <= item
+        int64_t lo = 0, hi = total_slots - 1;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) / 2;
+            if (a.start[mid] <= item) lo = mid; else hi = mid - 1;
+        }
+        // (the last slot whose start <= item is never empty: an empty slot shares
+        //  its start with the next slot, and item < total)
+        const int lvl = (int)(lo / a.nsys);
+        const int64_t k = lo - (int64_t)lvl * a.nsys;
+        const int64_t i = item - a.start[lo];
+        const int64_t n = a.offsets[k + 1] - a.offsets[k];
+        int K[kMaxLevels], H[kMaxLevels], Lw[kMaxLevels];
+        int64_t G[kMaxLevels], nwin[kMaxLevels];
+        const int P = rg_plan(n, a.cap, a.fuse, a.L, K, G, nwin, H, Lw);
+
+        // wait for the previous level of this system
+        if (threadIdx.x == 0) {
+            int skip = 0;
+            if (lvl > 0) {
+                const bool hook = a.inject && k == 0 && lvl == 1;
+                const unsigned need = (unsigned)a.count[(int64_t)(lvl - 1) * a.nsys + k] + (hook ? 1u : 0u);
+                const unsigned* ctr = a.done + (int64_t)(lvl - 1) * a.nsys + k;
+                const long long limit = a.inject ? kSpinLimitInjected : kSpinLimit;
+                long long it = 0;
+                while (ld_acquire(ctr) < need) {
+                    if (++it >= limit || *((volatile int*)a.err)) { skip = 1; atomicExch(a.err, 1); break; }
+                    __nanosleep(256);
+                }
+            }
+            s_skip = skip;
+        }
+        __syncthreads();
+        if (!s_skip) {
+            PcrPassArgs p;
+            const bool fin = lvl == P;
+            for (int u = 0; u < NSTATE; u++) {
+                p.src[u] = lvl == 0 ? (u < 6 ? a.src[u] : nullptr) : a.buf[(lvl - 1) & 1][u];
+                p.dst[u] = fin ? nullptr : a.buf[lvl & 1][u];
+            }
+            p.x = a.y;
+            p.offsets = a.offsets;
+            p.src_ss = 0; p.src_rs = 1; p.dst_ss = 0; p.dst_rs = 1;
+            p.n = n; p.m = a.nsys; p.G = G[lvl];
+            p.K = K[lvl]; p.final_step = fin ? 1 : 0; p.L = Lw[lvl]; p.H = H[lvl];
+            p.nwin = nwin[lvl];
+            p.TRmax = a.cap;
+            const int64_t r = fin ? i : i / nwin[lvl];
+            const int64_t w = fin ? 0 : i - r * nwin[lvl];
+            pcr_tile<kRgRPT, true>(p, k, r, w, smem);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(a.done + (int64_t)lvl * a.nsys + k, 1u);
+        }
+    }
+}
+
+// Cached CUDA graph of the launch sequence, per (device, stream, arguments).
+struct GraphKey {
+    int dev;
+    cudaStream_t s;
+    const void* ptrs[8];
+    int64_t nsys, max_rows;
+    int cap, fuse, L;
+    bool operator<(const GraphKey& o) const {
+        return std::tie(dev, s, ptrs[0], ptrs[1], ptrs[2], ptrs[3], ptrs[4], ptrs[5], ptrs[6], ptrs[7], nsys, max_rows, cap, fuse, L) <
+               std::tie(o.dev, o.s, o.ptrs[0], o.ptrs[1], o.ptrs[2], o.ptrs[3], o.ptrs[4], o.ptrs[5], o.ptrs[6], o.ptrs[7], o.nsys, o.max_rows, o.cap, o.fuse, o.L);
+    }
+};
+std::mutex g_graph_mu;
+std::map<GraphKey, cudaGraphExec_t> g_graphs;
+
+cudaError_t enqueue(const RgArgs& a, int grid, cudaStream_t s)
+{
+    const int pg = (int)std::min<int64_t>(std::max<int64_t>(1, cdiv64(a.nsys, 256)), 1024);
+    rg_plan_kernel<<<pg, 256, 0, s>>>(a);
+    rg_scan_kernel<<<1, 1024, 0, s>>>(a);
+    const size_t smem = (size_t)a.cap * 14 * sizeof(double);
+    rg_persistent_kernel<<<grid, kRgThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+pcrp_status ragged_mixed(const double* a, const double* b, const double* c, const double* d, const double* e,
+                         double* y, const int64_t* offsets, int64_t nsys, int64_t max_rows, double tol,
+                         int32_t max_sweeps, const pcrp_opts* o, cudaStream_t st);
+
+size_t ragged_workspace_bytes(int64_t nsys, int64_t total_rows)
+{
+    const size_t state = 2 * (size_t)NSTATE * (size_t)total_rows * sizeof(double);
+    const size_t plan = (size_t)kMaxLevels * nsys * (2 * sizeof(int64_t) + sizeof(unsigned)) + 2 * sizeof(int64_t) + 64;
+    return (state + 255) / 256 * 256 + plan + 256;
+}
+
+pcrp_status ragged_f64(const double* a, const double* b, const double* c, const double* d, const double* e,
+                       double* y, const int64_t* offsets, int64_t nsys, int64_t max_rows, const pcrp_opts* o,
+                       cudaStream_t st)
+{
+    int cap = std::min(PCRP_TUNED_SMEM_ROWS, kRgCap);
+    int fuse = PCRP_TUNED_FUSE_STRIDES, L = PCRP_TUNED_TILE_ROWS;
+    if (o && o->size >= sizeof(pcrp_opts)) {
+        if (o->smem_rows > 0) cap = std::min(o->smem_rows, kRgCap);
+        if (o->fuse_strides > 0) fuse = o->fuse_strides;
+        if (o->tile_rows > 0) L = o->tile_rows;
+    }
+    cap = std::max(cap, 8);
+    fuse = std::min(std::max(fuse, 1), 8);
+    while (2 * ((1 << fuse) - 1) + 1 > cap && fuse > 1) fuse--;
+    // levels needed by the largest system must fit the plan arrays
+    {
+        int ns = ref_strides(max_rows), s1 = 0;
+        while (s1 < ns && cdiv64(max_rows, int64_t(1) << s1) > cap) s1++;
+        if ((s1 + fuse - 1) / fuse + 1 > kMaxLevels) return set_error(PCRP_EINVAL, "pcrp_solve_ragged: max_rows too large");
+    }
+    // the call synchronises anyway: read and check the offsets on the host
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing(st, &cs);
+    if (ce != cudaSuccess) return cuda_error(ce, "cudaStreamIsCapturing");
+    if (cs != cudaStreamCaptureStatusNone)
+        return set_error(PCRP_ENOTSUP, "pcrp_solve_ragged synchronises and cannot be captured; it replays its own graph");
+    std::vector<int64_t> h_off((size_t)nsys + 1);
+    ce = cudaMemcpyAsync(h_off.data(), offsets, (nsys + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return cuda_error(ce, "pcrp_solve_ragged: reading offsets");
+    if (h_off[0] != 0) return set_error(PCRP_EINVAL, "pcrp_solve_ragged: offsets[0] = %lld, expected 0", (long long)h_off[0]);
+    for (int64_t k = 0; k < nsys; k++) {
+        const int64_t nk = h_off[k + 1] - h_off[k];
+        if (nk < 0 || nk > max_rows)
+            return set_error(PCRP_EINVAL, "pcrp_solve_ragged: system %lld has %lld rows (max_rows %lld)",
+                             (long long)k, (long long)nk, (long long)max_rows);
+    }
+    const int64_t total_rows_bound = std::max<int64_t>(h_off[nsys], 1);
+    void* ws = nullptr;
+    pcrp_status rc = get_workspace(o, ragged_workspace_bytes(nsys, total_rows_bound), st, &ws);
+    if (rc != PCRP_OK) return rc;
+
+    RgArgs A;
+    std::memset(&A, 0, sizeof A);
+    A.src[0] = a; A.src[1] = b; A.src[2] = c; A.src[3] = d; A.src[4] = e; A.src[5] = y;
+    A.y = y; A.offsets = offsets; A.nsys = nsys; A.cap = cap; A.fuse = fuse; A.L = L;
+    // failure-detection test hook (documented in the header): reserved0 == 0x7E57
+    A.inject = (o && o->size >= sizeof(pcrp_opts) && o->reserved0 == 0x7E57) ? 1 : 0;
+    char* base = static_cast<char*>(ws);
+    const size_t state_bytes = ((2 * (size_t)NSTATE * (size_t)total_rows_bound * sizeof(double)) + 255) / 256 * 256;
+    double* sb = reinterpret_cast<double*>(base);
+    for (int u = 0; u < 2; u++)
+        for (int q = 0; q < NSTATE; q++) A.buf[u][q] = sb + ((size_t)u * NSTATE + q) * (size_t)total_rows_bound;
+    char* pp = base + state_bytes;
+    A.count = reinterpret_cast<int64_t*>(pp); pp += (size_t)kMaxLevels * nsys * sizeof(int64_t);
+    A.start = reinterpret_cast<int64_t*>(pp); pp += ((size_t)kMaxLevels * nsys + 1) * sizeof(int64_t);
+    A.done = reinterpret_cast<unsigned*>(pp); pp += (size_t)kMaxLevels * nsys * sizeof(unsigned);
+    pp = base + ((pp - base) + 15) / 16 * 16;
+    A.head = reinterpret_cast<unsigned long long*>(pp); pp += 16;
+    A.err = reinterpret_cast<int*>(pp);
+
+    int dev = 0;
+    ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess) return cuda_error(ce, "cudaGetDevice");
+    const size_t smem = (size_t)cap * 14 * sizeof(double);
+    ce = cudaFuncSetAttribute(rg_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kRgCap * 14 * sizeof(double)));
+    if (ce != cudaSuccess) return cuda_error(ce, "cudaFuncSetAttribute");
+    int per_sm = 0, sms = 0;
+    ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rg_persistent_kernel, kRgThreads, smem);
+    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (ce != cudaSuccess) return cuda_error(ce, "occupancy query");
+    const int grid = std::max(1, per_sm * sms);
+
+    GraphKey key{};
+    key.dev = dev; key.s = st;
+    const void* ptrs[8] = {a, b, c, d, e, y, offsets, ws};
+    for (int q = 0; q < 8; q++) key.ptrs[q] = ptrs[q];
+    key.nsys = nsys; key.max_rows = max_rows; key.cap = cap; key.fuse = fuse; key.L = L + (A.inject << 20);
+    cudaGraphExec_t exec = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_graph_mu);
+        auto it = g_graphs.find(key);
+        if (it != g_graphs.end()) exec = it->second;
+    }
+    if (!exec) {
+        cudaStream_t cap_s = nullptr;
+        ce = cudaStreamCreateWithFlags(&cap_s, cudaStreamNonBlocking);
+        if (ce != cudaSuccess) return cuda_error(ce, "cudaStreamCreate");
+        cudaGraph_t g = nullptr;
+        ce = cudaStreamBeginCapture(cap_s, cudaStreamCaptureModeThreadLocal);
+        if (ce == cudaSuccess) {
+            cudaError_t le = enqueue(A, grid, cap_s);
+            ce = cudaStreamEndCapture(cap_s, &g);
+            if (ce == cudaSuccess) ce = le;
+        }
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        cudaStreamDestroy(cap_s);
+        if (ce != cudaSuccess) return cuda_error(ce, "ragged graph capture");
+        std::lock_guard<std::mutex> lk(g_graph_mu);
+        g_graphs[key] = exec;
+    }
+    ce = cudaGraphLaunch(exec, st);
+    if (ce != cudaSuccess) return cuda_error(ce, "cudaGraphLaunch");
+    count_launch(3);                       // the graph's three kernels
+    int err = 0;
+    ce = cudaMemcpyAsync(&err, A.err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return cuda_error(ce, "pcrp_solve_ragged");
+    if (err) return set_error(PCRP_ETIMEOUT, "pcrp_solve_ragged: a work-queue wait gave up");
+    return PCRP_OK;
+}
+
+}  // namespace pcrp
+
+using namespace pcrp;
+
+extern "C" pcrp_status pcrp_solve_ragged(const double* a, const double* b, const double* c, const double* d,
+                                         const double* e, double* y, const int64_t* offsets, int64_t nsys,
+                                         int64_t max_rows, int32_t mode, double tol, int32_t max_sweeps,
+                                         const pcrp_opts* opts, pcrp_stream stream)
+{
+    if (nsys < 0 || max_rows < 0) return set_error(PCRP_EINVAL, "pcrp_solve_ragged: negative size");
+    if (mode != 0 && mode != 1) return set_error(PCRP_EINVAL, "pcrp_solve_ragged: mode %d (0 FP64, 1 mixed)", mode);
+    if (nsys == 0 || max_rows == 0) return PCRP_OK;
+    if (!offsets || !a || !b || !c || !d || !e || !y) return set_error(PCRP_EINVAL, "pcrp_solve_ragged: null pointer");
+    if (nsys > (int64_t(1) << 24) || max_rows > (int64_t(1) << 31))
+        return set_error(PCRP_EINVAL, "pcrp_solve_ragged: size out of range");
+    if (mode == 0) return ragged_f64(a, b, c, d, e, y, offsets, nsys, max_rows, opts, (cudaStream_t)stream);
+    return ragged_mixed(a, b, c, d, e, y, offsets, nsys, max_rows, tol, max_sweeps, opts, (cudaStream_t)stream);
+}

@@ -1,0 +1,154 @@
+"""Autotuner for the tile sizes, fused-stride depth and shared/global split.
+
+Times every candidate configuration of the faithful FP64 path and of the
+mixed-precision path on representative batch shapes (CUDA events, median of
+several solves on a resident batch), keeps the fastest per size class, and
+writes
+
+  * a JSON record of every measurement (``--json``), and
+  * ``csrc/tuned_params.h`` (``--write``), whose tables the library compiles
+    in as its defaults (``pcrp_opts`` fields still override them per call).
+
+The FP64 results do not depend on the choice (every plan is bit-exact with the
+reference); the mixed results move only at rounding level.
+
+  python -m pcrp.autotune --json profiles/autotune_gb300.json --write
+"""
+from __future__ import annotations
+
+import argparse
+import itertools
+import json
+import os
+import statistics
+import time
+
+from . import GEN_DOMINANT, Opts, generate_device, solve_f64, solve_mixed
+from .build import CSRC
+
+# (size-class upper bound n_max, batch m used to time it)
+F64_CLASSES = [(1024, 1024), (8192, 256), (131072, 64), (1 << 21, 8)]
+MP_CLASSES = [(1024, 2048), (8192, 1024), (131072, 128), (1 << 21, 16)]
+
+
+def _timeit(fn, reps=3, warm=1):
+    import torch
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(warm):
+        fn()
+    out = []
+    for _ in range(reps):
+        e0.record(s)
+        fn()
+        e1.record(s)
+        e1.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return statistics.median(out)
+
+
+def _batch(m, n, seed=1):
+    import torch
+    arrs = [torch.empty(m * n, dtype=torch.float64, device="cuda") for _ in range(6)]
+    generate_device(GEN_DOMINANT, seed, m, n, 0, arrs)
+    return arrs
+
+
+def f64_candidates():
+    for smem, fuse, threads in itertools.product((512, 1024, 2048), (1, 2, 3, 4, 5), (128, 256)):
+        H = 2 * ((1 << fuse) - 1)
+        if smem - 2 * H < 64:
+            continue
+        yield dict(smem_rows=smem, fuse_strides=fuse, tile_rows=smem - 2 * H, threads=threads)
+
+
+def mp_candidates():
+    for cap, fuse in itertools.product((256, 512, 1024, 2048), (2, 3, 4, 5, 6, 7)):
+        if cap - 2 * ((1 << fuse) - 1) < 32:
+            continue
+        yield dict(smem_rows=2 * cap, fuse_strides=fuse)
+
+
+def tune(budget_s: float = 600.0, verbose: bool = True):
+    import torch
+    t_start = time.time()
+    rec = {"device": torch.cuda.get_device_name(0), "f64": [], "mixed": []}
+    for kind, classes, cands, solver in (("f64", F64_CLASSES, list(f64_candidates()), solve_f64),
+                                         ("mixed", MP_CLASSES, list(mp_candidates()), solve_mixed)):
+        for n_max, m in classes:
+            n = n_max if n_max <= 131072 else n_max // 2
+            arrs = _batch(m, n)
+            rhs = arrs[5].clone()
+            best = None
+            for c in cands:
+                if time.time() - t_start > budget_s:
+                    break
+                o = Opts(**c)
+
+                def run():
+                    arrs[5].copy_(rhs)
+                    if solver is solve_mixed:
+                        solver(*arrs, m, n, opts=o, report=False)
+                    else:
+                        solver(*arrs, m, n, opts=o)
+                try:
+                    ms = _timeit(run)
+                except Exception as exc:          # a candidate the library refuses
+                    rec[kind].append(dict(n=n, m=m, opts=c, error=str(exc)))
+                    continue
+                rec[kind].append(dict(n=n, m=m, opts=c, ms=ms, gunk_s=m * n / ms / 1e6))
+                if best is None or ms < best[0]:
+                    best = (ms, c)
+                if verbose:
+                    print(f"{kind} n={n} m={m} {c} {ms:.3f} ms", flush=True)
+            rec.setdefault(kind + "_best", []).append(dict(n_max=n_max, n=n, m=m, ms=best[0], opts=best[1]))
+            del arrs, rhs
+            torch.cuda.empty_cache()
+    return rec
+
+
+def header_text(rec) -> str:
+    f64 = rec["f64_best"]
+    mp = rec["mixed_best"]
+    rows_f = ", \\\n    ".join("{%d, %d, %d, %d, %d}" % (b["n_max"], b["opts"]["smem_rows"], b["opts"]["fuse_strides"],
+                                                     b["opts"]["tile_rows"], b["opts"]["threads"]) for b in f64)
+    rows_m = ", \\\n    ".join("{%d, %d, %d}" % (b["n_max"], b["opts"]["smem_rows"] // 2, b["opts"]["fuse_strides"])
+                            for b in mp)
+    return f"""// tuned_params.h -- defaults chosen by the autotuner (pcrp/autotune.py) on {rec['device']}.
+// Regenerated by `python -m pcrp.autotune --write`; edit there, not here.
+#pragma once
+#define PCRP_TUNED_SMEM_ROWS {f64[-1]['opts']['smem_rows']}     // ragged path: shared-memory capacity (rows)
+#define PCRP_TUNED_FUSE_STRIDES {f64[-1]['opts']['fuse_strides']}     // ragged path: strides fused per global pass
+#define PCRP_TUNED_TILE_ROWS {f64[-1]['opts']['tile_rows']}      // ragged path: rows written per CTA in a global pass
+#define PCRP_TUNED_THREADS {f64[-1]['opts']['threads']}        // threads per CTA
+#define PCRP_TUNED_MP_SMEM_BLOCKS {mp[-1]['opts']['smem_rows'] // 2}   // mixed: block rows solved whole in shared memory
+#define PCRP_TUNED_MP_FUSE {mp[-1]['opts']['fuse_strides']}            // mixed: FP32 block strides fused per global pass
+// FP64 path by system size: {{n_max, smem_rows, fuse_strides, tile_rows, threads}}
+#define PCRP_TUNED_F64_TABLE {{ \\
+    {rows_f} }}
+// mixed path by system size: {{n_max, block rows in shared memory, fuse_strides}}
+#define PCRP_TUNED_MP_TABLE {{ \\
+    {rows_m} }}
+"""
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--json", default=None)
+    ap.add_argument("--header", default=os.path.join(CSRC, "tuned_params.h"))
+    ap.add_argument("--write", action="store_true")
+    ap.add_argument("--budget", type=float, default=600.0)
+    args = ap.parse_args()
+    rec = tune(args.budget)
+    if args.json:
+        with open(args.json, "w") as f:
+            json.dump(rec, f, indent=1)
+    text = header_text(rec)
+    if args.write:
+        with open(args.header, "w") as f:
+            f.write(text)
+    print(text)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,140 @@
+"""GPU tests of the mixed-precision solver (FP32 2x2-block PCR + FP64
+refinement) against the FP64 elimination oracle.
+
+Bar (the solver's contract): relative forward error <= 1e-12 against the FP64
+banded Gaussian elimination on diagonally dominant systems, bands untouched,
+and an honest report (sweeps, estimate, residual)."""
+import numpy as np
+import pytest
+
+import oracle as O
+import pcrp
+from helpers import dd_bands, to_device, to_layout
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def run_mixed(arrs, m, n, layout=pcrp.CONTIGUOUS, dev="cuda:0", **kw):
+    import torch
+    t = to_device(arrs, dev)
+    info = pcrp.solve_mixed(*t, m, n, layout, **kw)
+    torch.cuda.synchronize()
+    return t[5].cpu().numpy(), info, t
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 7, 8, 31, 100, 512, 1000, 1024, 2047, 4096, 5001])
+@pytest.mark.parametrize("layout", [pcrp.CONTIGUOUS, pcrp.INTERLEAVED])
+def test_mixed_dominant_meets_tolerance(cuda, n, layout):
+    m = 6
+    arrs = to_layout(dd_bands(np.random.default_rng(n), m, n, garbage=True), m, n, layout)
+    x, info, _ = run_mixed(arrs, m, n, layout)
+    xg = O.ge(*arrs, m, n, layout)
+    assert O.fwd_err(x, xg, m, n, layout) <= TOL
+    assert info.converged == 1 and 1 <= info.sweeps <= 4
+    # residual of the FP64 answer relative to |A||x|: a few hundred ulps at most
+    assert info.resid < 1e-13
+
+
+@pytest.mark.parametrize("kind,m,n", [
+    (pcrp.GEN_DOMINANT, 64, 512), (pcrp.GEN_DOMINANT, 4, 65536), (pcrp.GEN_ADI, 32, 4096),
+    (pcrp.GEN_WEAK, 8, 8192), (pcrp.GEN_WEAK, 2, 1 << 20), (pcrp.GEN_DOMINANT, 3, 1 << 20),
+])
+def test_mixed_benchmark_generators(cuda, kind, m, n):
+    arrs = pcrp.generate(kind, 17, m, n)
+    x, info, _ = run_mixed(arrs, m, n)
+    xg = O.ge(*arrs, m, n)
+    assert O.fwd_err(x, xg, m, n) <= TOL, (info.sweeps, info.fwd_err_est)
+    assert info.converged == 1
+
+
+@pytest.mark.parametrize("opts", [dict(smem_rows=64), dict(smem_rows=64, fuse_strides=2), dict(smem_rows=8, fuse_strides=1)])
+def test_mixed_forced_global_passes(cuda, opts):
+    m, n = 3, 3000
+    arrs = dd_bands(np.random.default_rng(7), m, n)
+    x, info, _ = run_mixed(arrs, m, n, opts=pcrp.Opts(**opts))
+    assert O.fwd_err(x, O.ge(*arrs, m, n), m, n) <= TOL
+    assert info.converged == 1
+
+
+def test_mixed_ill_conditioned_adi(cuda):
+    """ADI at n = 65536: entries reach ~1e6 against a unit dominance margin
+    (condition ~1e6).  FP32 corrections contract slowly (rho ~ 1e-2) and the
+    FP64 residual itself limits the attainable accuracy to ~cond*eps, so a
+    1e-12 target is out of reach: the solver must say so (PCRP_ENOCONV) rather
+    than claim it, and it must converge to a 1e-9 target, agreeing with FP64
+    elimination (itself only good to ~cond*eps) to that level."""
+    m, n = 4, 65536
+    arrs = pcrp.generate(pcrp.GEN_ADI, 17, m, n)
+    with pytest.raises(pcrp.PcrpError) as ei:
+        run_mixed(arrs, m, n, max_sweeps=12)
+    assert ei.value.status == 5
+    x, info, _ = run_mixed(arrs, m, n, tol=1e-9, max_sweeps=16)
+    assert info.converged == 1 and info.sweeps >= 3
+    assert O.fwd_err(x, O.ge(*arrs, m, n), m, n) <= 1e-9
+
+
+def test_mixed_solves_what_the_reference_algorithm_cannot(cuda):
+    """Exact zeros among the off-diagonals break PCR-Penta's pivots
+    (kernel.cu:72-75); the block pivots of the mixed solver do not care."""
+    rng = np.random.default_rng(5)
+    m, n = 3, 256
+    a, b, d, e = [rng.integers(-8, 9, (m, n)) / 8.0 for _ in range(4)]
+    a[:, :2] = 0; b[:, :1] = 0; d[:, -1:] = 0; e[:, -2:] = 0
+    c = np.abs(a) + np.abs(b) + np.abs(d) + np.abs(e) + 1.0
+    xt = rng.integers(-64, 65, (m, n)).astype(np.float64)
+    y = c * xt
+    y[:, 2:] += a[:, 2:] * xt[:, :-2]; y[:, 1:] += b[:, 1:] * xt[:, :-1]
+    y[:, :-1] += d[:, :-1] * xt[:, 1:]; y[:, :-2] += e[:, :-2] * xt[:, 2:]
+    arrs = [v.ravel().copy() for v in (a, b, c, d, e, y)]
+    x, info, _ = run_mixed(arrs, m, n)
+    assert O.fwd_err(x, xt.ravel(), m, n) <= TOL
+    assert O.fwd_err(O.pcr(*arrs, m, n), xt.ravel(), m, n) > 1e-3
+
+
+def test_mixed_async_equals_reported(cuda):
+    import torch
+    m, n = 5, 9000
+    arrs = dd_bands(np.random.default_rng(9), m, n)
+    x1, info, _ = run_mixed(arrs, m, n)
+    t = to_device(arrs, cuda)
+    pcrp.solve_mixed(*t, m, n, report=False)
+    torch.cuda.synchronize()
+    x2 = t[5].cpu().numpy()
+    assert O.fwd_err(x2, O.ge(*arrs, m, n), m, n) <= TOL
+    assert O.fwd_err(x1, x2, m, n) <= TOL
+
+
+def test_mixed_reports_nonconvergence(cuda):
+    m, n = 2, 700
+    arrs = dd_bands(np.random.default_rng(3), m, n)
+    with pytest.raises(pcrp.PcrpError) as ei:
+        run_mixed(arrs, m, n, max_sweeps=1)
+    assert ei.value.status == 5
+
+
+def test_mixed_leaves_bands_untouched(cuda):
+    import torch
+    m, n = 3, 5000
+    arrs = dd_bands(np.random.default_rng(4), m, n)
+    t = to_device(arrs, cuda)
+    before = [v.clone() for v in t[:5]]
+    pcrp.solve_mixed(*t, m, n)
+    torch.cuda.synchronize()
+    for u, v in zip(before, t[:5]):
+        assert torch.equal(u, v)
+
+
+@pytest.mark.parametrize("layout", [pcrp.CONTIGUOUS, pcrp.INTERLEAVED])
+def test_residual_f64_matches_oracle(cuda, layout):
+    import torch
+    m, n = 4, 777
+    arrs = to_layout(dd_bands(np.random.default_rng(2), m, n, garbage=True), m, n, layout)
+    x = np.random.default_rng(3).uniform(-1, 1, m * n)
+    t = to_device(arrs + [x, np.zeros(m * n)], cuda)
+    pcrp.residual_f64(*t[:6], t[6], t[7], m, n, layout)
+    torch.cuda.synchronize()
+    r = t[7].cpu().numpy()
+    ro = O.residual(*arrs, x, m, n, layout)
+    scale = np.abs(arrs[2]).max() * np.abs(x).max()
+    assert np.abs(r - ro).max() <= 8 * np.finfo(float).eps * scale

@@ -1,0 +1,104 @@
+"""Ragged batches through pcrp_solve_ragged: one persistent kernel (cached
+CUDA graph) over systems of uneven size.  FP64 mode must equal the faithful
+per-system solve bit for bit; mixed mode must meet the 1e-12 forward-error
+bar against elimination."""
+import numpy as np
+import pytest
+
+import oracle as O
+import pcrp
+from helpers import assert_bitexact, dd_bands
+
+pytestmark = pytest.mark.gpu
+
+
+def ragged_batch(sizes, seed, garbage=True):
+    rng = np.random.default_rng(seed)
+    parts = [dd_bands(rng, 1, int(s), garbage=garbage) for s in sizes]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    arrs = [np.concatenate([p[k] for p in parts]) for k in range(6)]
+    return arrs, offs
+
+
+def run_ragged(arrs, offs, mode=0, opts=None, dev="cuda:0", **kw):
+    import torch
+    t = [torch.from_numpy(v).to(dev) for v in arrs]
+    o = torch.from_numpy(offs).to(dev)
+    sizes = np.diff(offs)
+    pcrp.solve_ragged(*t, o, len(sizes), int(sizes.max()), mode=mode, opts=opts, **kw)
+    torch.cuda.synchronize()
+    return t[5].cpu().numpy()
+
+
+SIZES = [1, 2, 3, 5, 7, 32, 100, 511, 512, 1000, 1024, 1025, 2048, 3000, 4096, 9000, 65536, 17, 1100]
+
+
+@pytest.mark.parametrize("opts", [None, dict(smem_rows=64), dict(smem_rows=128, fuse_strides=2, tile_rows=50)])
+def test_ragged_f64_bitexact_per_system(cuda, opts):
+    arrs, offs = ragged_batch(SIZES, 1)
+    x = run_ragged(arrs, offs, 0, pcrp.Opts(**opts) if opts else None)
+    xo = O.ragged(*arrs, offs[:-1], np.diff(offs), kind="pcr")
+    assert_bitexact(x, xo, f"ragged f64 {opts}")
+
+
+def test_ragged_f64_log_uniform_sizes_match_uniform_path(cuda):
+    import torch
+    sizes = pcrp.ragged_sizes(3, 256, 32, 65536)
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    arrs = pcrp.generate_ragged(pcrp.GEN_DOMINANT, 3, offs)
+    x1 = run_ragged(arrs, offs, 0)
+    x2 = run_ragged(arrs, offs, 0)                    # graph replay
+    assert np.array_equal(x1, x2)
+    for k in range(0, len(sizes), 37):
+        sl = slice(offs[k], offs[k + 1])
+        t = [torch.from_numpy(np.ascontiguousarray(v[sl])).to(cuda) for v in arrs]
+        pcrp.solve_f64(*t, 1, int(sizes[k]))
+        torch.cuda.synchronize()
+        assert_bitexact(x1[sl], t[5].cpu().numpy(), f"system {k} n={sizes[k]}")
+
+
+def test_ragged_rejects_bad_offsets(cuda):
+    import torch
+    arrs, offs = ragged_batch([5, 6], 2)
+    bad = offs.copy(); bad[0] = 1
+    with pytest.raises(pcrp.PcrpError) as ei:
+        run_ragged(arrs, bad)
+    assert ei.value.status == 1
+    t = [torch.from_numpy(v).to(cuda) for v in arrs]
+    o = torch.from_numpy(offs).to(cuda)
+    with pytest.raises(pcrp.PcrpError):
+        pcrp.solve_ragged(*t, o, 2, 5)                   # max_rows below a system's size
+
+
+def test_ragged_wait_timeout_is_reported(cuda):
+    """Failure detection: the test hook makes one dependency wait unsatisfiable;
+    the bounded wait gives up, the kernel returns, the call reports ETIMEOUT and
+    the context stays usable."""
+    arrs, offs = ragged_batch([5000, 30], 4)
+    with pytest.raises(pcrp.PcrpError) as ei:
+        run_ragged(arrs, offs, 0, pcrp.Opts(reserved0=0x7E57))
+    assert ei.value.status == 4
+    x = run_ragged(arrs, offs, 0)                     # still works afterwards
+    assert_bitexact(x, O.ragged(*arrs, offs[:-1], np.diff(offs), kind="pcr"), "after timeout")
+
+
+def test_ragged_mixed_meets_tolerance(cuda):
+    arrs, offs = ragged_batch(SIZES, 5)
+    x = run_ragged(arrs, offs, 1)
+    xg = O.ragged(*arrs, offs[:-1], np.diff(offs), kind="ge")
+    for k in range(len(SIZES)):
+        sl = slice(offs[k], offs[k + 1])
+        assert O.fwd_err(x[sl], xg[sl], 1, int(SIZES[k])) <= 1e-12, k
+
+
+def test_ragged_mixed_log_uniform(cuda):
+    sizes = pcrp.ragged_sizes(9, 300, 32, 65536)
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    arrs = pcrp.generate_ragged(pcrp.GEN_DOMINANT, 9, offs)
+    x1 = run_ragged(arrs, offs, 1)
+    x2 = run_ragged(arrs, offs, 1)                    # graph replay
+    assert np.array_equal(x1, x2)
+    xg = O.ragged(*arrs, offs[:-1], sizes, kind="ge")
+    worst = max(O.fwd_err(x1[offs[k]:offs[k + 1]], xg[offs[k]:offs[k + 1]], 1, int(sizes[k]))
+                for k in range(len(sizes)))
+    assert worst <= 1e-12
