@@ -165,6 +165,7 @@ def run_reference(args, world, rank):
 
 
 def run_ours(args, world, rank, local, pg):
+    import numpy as np
     import torch
     import pcrp
 
@@ -182,8 +183,9 @@ def run_ours(args, world, rank, local, pg):
         pcrp.generate_device(cfg["kind"], seed, m, n, pcrp.CONTIGUOUS, arrs, stream=stream)
         rhs = arrs[5].clone()
     stream.synchronize()
-    solve = (lambda: pcrp.solve_f64(*arrs, m, n, stream=stream)) if args.solver == "f64" else \
-        (lambda: pcrp.solve_mixed(*arrs, m, n, stream=stream, report=False))
+    opts = pcrp.Opts(**json.loads(args.opts)) if args.opts else None
+    solve = (lambda: pcrp.solve_f64(*arrs, m, n, stream=stream, opts=opts)) if args.solver == "f64" else \
+        (lambda: pcrp.solve_mixed(*arrs, m, n, stream=stream, report=False, opts=opts))
 
     def step():
         arrs[5].copy_(rhs, non_blocking=True)
@@ -266,17 +268,49 @@ def run_ours(args, world, rank, local, pg):
                                          if other_solver == "mixed" else
                                          (world * m * n / (kms_med * 1e-3) / 1e9) / other["value"])
 
-    # end to end through the public API with host buffers (pinned)
+    # library comparison point: cuSPARSE gpsvInterleavedBatch (QR, FP64) on the
+    # same systems in the interleaved layout it requires (the transposes and the
+    # fresh band copies it needs, since it overwrites them, are outside the timing)
+    lib_cmp = None
+    if args.cusparse:
+        import pcrp.compare as cmpmod
+        inter = [v.view(m, n).t().contiguous().view(-1) for v in arrs[:5]] + [rhs.view(m, n).t().contiguous().view(-1)]
+        work = [torch.empty_like(v) for v in inter]
+        import ctypes
+        L = cmpmod.lib()
+        nbytes = ctypes.c_size_t(0)
+        L.cmp_gpsv_buffer_size(*[w.data_ptr() for w in work], n, m, ctypes.byref(nbytes))
+        gbuf = torch.empty(max(1, int(nbytes.value)), dtype=torch.uint8, device=dev)
+        gms = []
+        with torch.cuda.stream(stream):
+            for it in range(max(3, args.steps) + 1):
+                for w, v in zip(work, inter):
+                    w.copy_(v, non_blocking=True)
+                ek0.record(stream)
+                rc = L.cmp_gpsv_solve(*[w.data_ptr() for w in work], n, m, gbuf.data_ptr(), stream.cuda_stream)
+                ek1.record(stream)
+                ek1.synchronize()
+                if rc:
+                    raise RuntimeError(f"cusparseDgpsvInterleavedBatch status {rc}")
+                if it >= 1:
+                    gms.append(ek0.elapsed_time(ek1))
+        lib_cmp = {"library": "cuSPARSE cusparseDgpsvInterleavedBatch (FP64, interleaved layout)",
+                   "ms_per_solve": statistics.median(gms),
+                   "value": world * m * n / (statistics.median(gms) * 1e-3) / 1e9}
+        x_gpsv = work[5].view(n, m).t()[: min(m, 16)].contiguous().view(-1).cpu().numpy()
+        del inter, work, gbuf
+
+    # end to end through the public API with host buffers (pinned): pcrp_solve_host
+    # copies each step's six input arrays in and the solution out, in chunks
+    # that overlap the solves; y is solved in place (the next step's rhs is the
+    # previous solution, same work)
     h_in = [torch.empty(m * n, dtype=torch.float64, pin_memory=True) for _ in range(6)]
     pcrp.generate_into(cfg["kind"], seed, m, n, pcrp.CONTIGUOUS, h_in)
-    h_out = torch.empty(m * n, dtype=torch.float64, pin_memory=True)
     e_steps = max(2, min(args.steps, 5))
+    precision = 0 if args.solver == "f64" else 1
 
     def e2e_step():
-        for d, h in zip(arrs, h_in):
-            d.copy_(h, non_blocking=True)
-        solve()
-        h_out.copy_(arrs[5], non_blocking=True)
+        pcrp.solve_host(*h_in, m, n, precision=precision, stream=stream)
 
     with torch.cuda.stream(stream):
         e2e_step()
@@ -310,6 +344,7 @@ def run_ours(args, world, rank, local, pg):
                    "l2": "inputs larger than L2 (0.8 GB vs 129 MB), no flush",
                    "parallelism": f"replicas x{world} (independent systems per GPU)"},
         "gpu_launches": launches,
+        "opts": json.loads(args.opts) if args.opts else "autotuned defaults",
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 6 * 8 * m * n,
                 "d2h_bytes_per_step": 8 * m * n, "ms_per_step": e_ms},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -320,6 +355,8 @@ def run_ours(args, world, rank, local, pg):
     }
     if other is not None:
         line["compare"] = other
+    if lib_cmp is not None:
+        line["library_baseline"] = lib_cmp
     if args.cpu_baseline and world == 1:
         if other is not None:
             # check the mixed solution against FP64 elimination on the first systems
@@ -327,7 +364,16 @@ def run_ours(args, world, rank, local, pg):
             import oracle as O
             ms = min(m, 16)
             host = pcrp.generate(cfg["kind"], seed, ms, n)
-            line["compare"]["fwd_err_vs_ge"] = O.fwd_err(x_mixed, O.ge(*host, ms, n), ms, n)
+            x_ge = O.ge(*host, ms, n)
+            xm64 = np.asarray(x_mixed, dtype=np.float64).reshape(ms, n)
+            xg64 = np.asarray(x_ge, dtype=np.float64).reshape(ms, n)
+            line["compare"]["fwd_err_vs_ge"] = float((np.abs(xm64 - xg64).max(axis=1) /
+                                                      np.maximum(np.abs(xg64).max(axis=1), 1e-300)).max())
+            line["compare"]["abs_max"] = [float(abs(x_mixed).max()), float(abs(x_ge).max())]
+            if lib_cmp is not None:
+                xc64 = np.asarray(x_gpsv, dtype=np.float64).reshape(ms, n)
+                line["library_baseline"]["fwd_err_vs_ge"] = float((np.abs(xc64 - xg64).max(axis=1) /
+                                                                   np.maximum(np.abs(xg64).max(axis=1), 1e-300)).max())
             line["compare"]["fwd_err_sample"] = f"first {ms} systems vs FP64 banded elimination"
         v, cores, dt = cpu_sample_gunk(cfg, min(m, args.ref_systems))
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -414,7 +460,10 @@ def main():
     ap.add_argument("--solver", choices=["f64", "mixed"], default="f64")
     ap.add_argument("--ref-systems", type=int, default=32)
     ap.add_argument("--m", type=int, default=0, help="override the number of systems (profiling runs)")
+    ap.add_argument("--opts", default="", help='tuning overrides as JSON, e.g. {"smem_rows": 1024}')
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-cusparse", dest="cusparse", action="store_false",
+                    help="skip timing cuSPARSE gpsvInterleavedBatch on the same systems")
     ap.add_argument("--no-compare", dest="compare", action="store_false",
                     help="skip timing the other precision on the same inputs")
     args = ap.parse_args()

@@ -161,6 +161,22 @@ pcrp_status pcrp_residual_f64(const double* a, const double* b, const double* c,
                               const double* x, double* r,
                               int64_t m, int64_t n, int32_t layout, pcrp_stream stream);
 
+/* Solves a batch that lives in HOST memory: a..e and y are host arrays of
+ * m*n doubles (page-locked memory lets the copies run asynchronously).  The
+ * systems are streamed through the GPU in chunks on two internal streams, so
+ * the host<->device copies of one chunk overlap the solve of another; y
+ * receives the solution.  precision 0 = pcrp_solve_f64 (bit-identical
+ * results), 1 = pcrp_solve_mixed (tol, max_sweeps as there; no report).
+ * Asynchronous on `stream`: the host arrays must stay valid until the stream
+ * reaches the end of the call.  opts->workspace, if given, holds the staging
+ * chunks (two chunks of 6 arrays).  No counterpart in the reference (its host
+ * code never moves data; this is the path of a caller whose batch is on the host). */
+pcrp_status pcrp_solve_host(const double* a, const double* b, const double* c,
+                            const double* d, const double* e, double* y,
+                            int64_t m, int64_t n, int32_t layout,
+                            int32_t precision, double tol, int32_t max_sweeps,
+                            const pcrp_opts* opts, pcrp_stream stream);
+
 /* ------------------------------------------------------------------------ */
 /* Ragged batches                                                           */
 /* ------------------------------------------------------------------------ */

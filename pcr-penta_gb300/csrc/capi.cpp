@@ -222,6 +222,7 @@ pcrp_status pcrp_solve_f64(const double* a, const double* b, const double* c, co
                            const double* e, double* y, int64_t m, int64_t n, int32_t layout,
                            const pcrp_opts* opts, pcrp_stream stream)
 {
+    NvtxRange nv("pcrp_solve_f64");
     return f64_solve(a, b, c, d, e, y, m, n, layout, opts, (cudaStream_t)stream, false, false, "pcrp_solve_f64");
 }
 
@@ -229,6 +230,7 @@ pcrp_status pcrp_solve_f64_small(const double* a, const double* b, const double*
                                  const double* e, double* y, int64_t m, int64_t n, int32_t layout,
                                  const pcrp_opts* opts, pcrp_stream stream)
 {
+    NvtxRange nv("pcrp_solve_f64_small");
     return f64_solve(a, b, c, d, e, y, m, n, layout, opts, (cudaStream_t)stream, true, false, "pcrp_solve_f64_small");
 }
 
@@ -236,6 +238,7 @@ pcrp_status pcrp_solve_f64_split(const double* a, const double* b, const double*
                                  const double* e, double* y, int64_t m, int64_t n, int32_t layout,
                                  const pcrp_opts* opts, pcrp_stream stream)
 {
+    NvtxRange nv("pcrp_solve_f64_split");
     return f64_solve(a, b, c, d, e, y, m, n, layout, opts, (cudaStream_t)stream, false, true, "pcrp_solve_f64_split");
 }
 

@@ -25,10 +25,10 @@
 // pipe, and every FP64<->FP32 conversion here is integer bit arithmetic
 // (no F2F instructions, which also issue on the FP64 pipe).
 //
-// Stopping rule.  With dx_s the correction of sweep s, the contraction
-// rho = |dx_s| / |dx_{s-1}| bounds the error left after applying dx_s by
-// about rho/(1-rho)*|dx_s|; a system is done when rho < 0.5 and twice that
-// bound is <= tol*|x|.
+// Stopping rule.  With dx_s the correction of sweep s, a system is done when
+// |dx_s| <= tol/2 |x| (the correction bounds what it leaves), or when the
+// corrections contract (rho = |dx_s|/|dx_{s-1}| < 0.5) and twice the
+// geometric tail rho/(1-rho)|dx_s| is <= tol |x|.
 // Each kernel reads the per-system norms left by the previous kernel, so the
 // decision needs no host round trip; finished systems skip all later work.
 #include <algorithm>
@@ -43,6 +43,16 @@ namespace {
 
 constexpr float kTrunc = 1e-10f;
 constexpr int kMpThreads = 256;
+// grid-stride kernels launch about one wave: a sweep whose systems have all
+// finished then costs a few microseconds per kernel
+int mp_grid_cap(const void* kernel, int threads, size_t smem)
+{
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 152 * 2;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 152 * 2;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess || per < 1) per = 1;
+    return sms * per;
+}
 
 // ---------------------------------------------------------------------------
 // integer-pipe conversions
@@ -168,12 +178,9 @@ mp_prep_kernel(MpArgs p)
         const M2 L = mmul(Mi, B.L), U = mmul(Mi, B.U);
         const float y0 = d2f_scaled(p.y[base + 2 * k * p.rs], B.sh0);
         const float y1 = 2 * k + 1 < p.n ? d2f_scaled(p.y[base + (2 * k + 1) * p.rs], B.sh1) : 0.0f;
-        float* s = p.S0;
-        const int64_t T = total;
-        s[0 * T + q] = L.m0; s[1 * T + q] = L.m1; s[2 * T + q] = L.m2; s[3 * T + q] = L.m3;
-        s[4 * T + q] = U.m0; s[5 * T + q] = U.m1; s[6 * T + q] = U.m2; s[7 * T + q] = U.m3;
-        p.R[q] = fmaf(Mi.m0, y0, Mi.m1 * y1);
-        p.R[T + q] = fmaf(Mi.m2, y0, Mi.m3 * y1);
+        p.S0[2 * q] = make_float4(L.m0, L.m1, L.m2, L.m3);
+        p.S0[2 * q + 1] = make_float4(U.m0, U.m1, U.m2, U.m3);
+        p.R[q] = make_float2(fmaf(Mi.m0, y0, Mi.m1 * y1), fmaf(Mi.m2, y0, Mi.m3 * y1));
     }
     if (blockIdx.x == 0) {
         for (int64_t j = threadIdx.x; j < p.m; j += blockDim.x) {
@@ -189,20 +196,52 @@ mp_prep_kernel(MpArgs p)
 // ---------------------------------------------------------------------------
 // FP32 block PCR pass (windows + halos at block level G, or whole subsystems)
 // ---------------------------------------------------------------------------
-template <int RPT>
-__global__ void __launch_bounds__(kMpThreads)
-mp_pass_kernel(MpPassArgs p)
+// Copy of the decoupled rows of a system whose couplings already vanished:
+// X = Y (final: write dx and its maximum) or the rhs carried to the next level
+// (non-final).  Item r of the G items of system j takes a contiguous range of
+// block rows, so the accesses coalesce whatever the gather stride.
+__device__ __forceinline__ void mp_copy_item(const MpPassArgs& p, int64_t j, int64_t r, int64_t w)
 {
-    extern __shared__ float fsm[];
-    const int TRm = p.TRmax;
-    __shared__ unsigned s_max[2];
+    const int64_t nb = p.nb;
+    const int64_t parts = p.G * p.nwin;
+    const int64_t part = r * p.nwin + w;
+    const int64_t per = (nb + parts - 1) / parts;
+    const int64_t k0 = part * per, k1 = min(k0 + per, nb);
+    float lmax = 0.0f;
+    for (int64_t kb = k0 + threadIdx.x; kb < k1; kb += blockDim.x) {
+        const int64_t q = j * nb + kb;
+        const float2 yv = p.srcY[q];
+        if (p.final_step) {
+            const int64_t i0 = 2 * kb;
+            p.dx[j * p.n + i0] = yv.x;
+            lmax = fmaxf(lmax, fabsf(yv.x));
+            if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = yv.y; lmax = fmaxf(lmax, fabsf(yv.y)); }
+        } else {
+            p.dstY[q] = yv;
+        }
+    }
+    if (p.final_step) {
+        lmax = warp_max(lmax);
+        if ((threadIdx.x & 31) == 0) atomic_max_pos(&p.ndx[(int64_t)p.sweep * p.m + j], lmax);
+    } else if (threadIdx.x == 0 && p.trunc_out && r == 0 && w == 0) {
+        atomicMax(&p.trunc_out[j], p.trunc_in[j]);         // stays below the threshold
+    }
+}
 
-    const int64_t blk = blockIdx.x;
-    const int64_t item = blk / p.nwin;
-    const int64_t w = blk - item * p.nwin;
-    const int64_t j = item / p.G;
-    const int64_t r = item - j * p.G;
-    if (p.fin[j]) return;
+__device__ __forceinline__ float amax4(const float4& v) {
+    return fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
+}
+__device__ __forceinline__ M2 m2(const float4& v) { return {v.x, v.y, v.z, v.w}; }
+__device__ __forceinline__ float4 f4(const M2& a) { return make_float4(a.m0, a.m1, a.m2, a.m3); }
+
+// One window (or whole subsystem) of one FP32 block-PCR pass.  Shared memory
+// holds two buffers of TRmax block rows, each row 3 float4 (L, U, Y + pad):
+// vector accesses, conflict-free at the 48-byte row pitch.
+template <int RPT>
+__device__ __forceinline__ void mp_pass_item(const MpPassArgs& p, int64_t j, int64_t r, int64_t w,
+                                             float4* fsm, unsigned* s_max)
+{
+    const int TRm = p.TRmax;
     const int64_t nb = p.nb;
     if (r >= nb) return;
     const int64_t nr = (nb - 1 - r) / p.G + 1;
@@ -214,18 +253,16 @@ mp_pass_kernel(MpPassArgs p)
     const int TR = (int)(t1 - t0);
     const int tid = threadIdx.x, bd = blockDim.x;
     const int64_t g0 = j * nb + r;                 // block row of local t = 0
-    // a system whose couplings vanished in an earlier pass needs no more strides
-    const bool truncated = p.trunc_in && __uint_as_float(p.trunc_in[j]) < kTrunc;
-    const int K = truncated ? 0 : p.K;
+    const int K = p.K;
 
     for (int q = 0; q < RPT; q++) {
         const int k = tid + q * bd;
         if (k < TR) {
             const int64_t gi = g0 + (t0 + k) * p.G;
-            float* s = fsm;
-            for (int u = 0; u < 8; u++) s[u * TRm + k] = p.srcLU[u][gi];
-            s[8 * TRm + k] = p.srcY[0][gi];
-            s[9 * TRm + k] = p.srcY[1][gi];
+            const float2 yv = p.srcY[gi];
+            fsm[3 * k] = p.srcLU[2 * gi];
+            fsm[3 * k + 1] = p.srcLU[2 * gi + 1];
+            fsm[3 * k + 2] = make_float4(yv.x, yv.y, 0.0f, 0.0f);
         }
     }
     if (tid == 0) { s_max[0] = 0u; s_max[1] = 0u; }
@@ -240,47 +277,43 @@ mp_pass_kernel(MpPassArgs p)
             const int64_t rem = (int64_t(1) << p.K) - (int64_t(2) << st);   // block halo = 2^K - 1
             rlo = max(wlo - rem, (int64_t)0); rhi = min(whi + rem, nr);
         }
-        const float* S = fsm + cur * 10 * TRm;
-        float* N = fsm + (cur ^ 1) * 10 * TRm;
+        const float4* S = fsm + cur * 3 * TRm;
+        float4* N = fsm + (cur ^ 1) * 3 * TRm;
         float lmax = 0.0f;
         for (int q = 0; q < RPT; q++) {
             const int k = tid + q * bd;
             const int64_t t = t0 + k;
             if (k < TR && t >= rlo && t < rhi) {
-                const M2 Lk = {S[0 * TRm + k], S[1 * TRm + k], S[2 * TRm + k], S[3 * TRm + k]};
-                const M2 Uk = {S[4 * TRm + k], S[5 * TRm + k], S[6 * TRm + k], S[7 * TRm + k]};
-                float y0 = S[8 * TRm + k], y1 = S[9 * TRm + k];
+                const M2 Lk = m2(S[3 * k]), Uk = m2(S[3 * k + 1]);
+                const float4 yk = S[3 * k + 2];
+                float y0 = yk.x, y1 = yk.y;
                 M2 Dn = {1.0f, 0.0f, 0.0f, 1.0f}, Ln = {0, 0, 0, 0}, Un = {0, 0, 0, 0};
                 if (t - dl >= 0) {
-                    const int km = k - dl;
-                    const M2 Lm = {S[0 * TRm + km], S[1 * TRm + km], S[2 * TRm + km], S[3 * TRm + km]};
-                    const M2 Um = {S[4 * TRm + km], S[5 * TRm + km], S[6 * TRm + km], S[7 * TRm + km]};
-                    const float ym0 = S[8 * TRm + km], ym1 = S[9 * TRm + km];
+                    const int km = 3 * (k - dl);
+                    const M2 Lm = m2(S[km]), Um = m2(S[km + 1]);
+                    const float4 ym = S[km + 2];
                     const M2 LU = mmul(Lk, Um), LL = mmul(Lk, Lm);
                     Dn = {Dn.m0 - LU.m0, Dn.m1 - LU.m1, Dn.m2 - LU.m2, Dn.m3 - LU.m3};
                     Ln = {-LL.m0, -LL.m1, -LL.m2, -LL.m3};
-                    y0 = fmaf(-Lk.m0, ym0, fmaf(-Lk.m1, ym1, y0));
-                    y1 = fmaf(-Lk.m2, ym0, fmaf(-Lk.m3, ym1, y1));
+                    y0 = fmaf(-Lk.m0, ym.x, fmaf(-Lk.m1, ym.y, y0));
+                    y1 = fmaf(-Lk.m2, ym.x, fmaf(-Lk.m3, ym.y, y1));
                 }
                 if (t + dl <= nr - 1) {
-                    const int kp = k + dl;
-                    const M2 Lp = {S[0 * TRm + kp], S[1 * TRm + kp], S[2 * TRm + kp], S[3 * TRm + kp]};
-                    const M2 Up = {S[4 * TRm + kp], S[5 * TRm + kp], S[6 * TRm + kp], S[7 * TRm + kp]};
-                    const float yp0 = S[8 * TRm + kp], yp1 = S[9 * TRm + kp];
+                    const int kp = 3 * (k + dl);
+                    const M2 Lp = m2(S[kp]), Up = m2(S[kp + 1]);
+                    const float4 yp = S[kp + 2];
                     const M2 UL = mmul(Uk, Lp), UU = mmul(Uk, Up);
                     Dn = {Dn.m0 - UL.m0, Dn.m1 - UL.m1, Dn.m2 - UL.m2, Dn.m3 - UL.m3};
                     Un = {-UU.m0, -UU.m1, -UU.m2, -UU.m3};
-                    y0 = fmaf(-Uk.m0, yp0, fmaf(-Uk.m1, yp1, y0));
-                    y1 = fmaf(-Uk.m2, yp0, fmaf(-Uk.m3, yp1, y1));
+                    y0 = fmaf(-Uk.m0, yp.x, fmaf(-Uk.m1, yp.y, y0));
+                    y1 = fmaf(-Uk.m2, yp.x, fmaf(-Uk.m3, yp.y, y1));
                 }
                 const M2 Mi = minv(Dn);
-                const M2 L2 = mmul(Mi, Ln), U2 = mmul(Mi, Un);
-                N[0 * TRm + k] = L2.m0; N[1 * TRm + k] = L2.m1; N[2 * TRm + k] = L2.m2; N[3 * TRm + k] = L2.m3;
-                N[4 * TRm + k] = U2.m0; N[5 * TRm + k] = U2.m1; N[6 * TRm + k] = U2.m2; N[7 * TRm + k] = U2.m3;
-                N[8 * TRm + k] = fmaf(Mi.m0, y0, Mi.m1 * y1);
-                N[9 * TRm + k] = fmaf(Mi.m2, y0, Mi.m3 * y1);
-                lmax = fmaxf(lmax, fmaxf(fmaxf(fmaxf(fabsf(L2.m0), fabsf(L2.m1)), fmaxf(fabsf(L2.m2), fabsf(L2.m3))),
-                                         fmaxf(fmaxf(fabsf(U2.m0), fabsf(U2.m1)), fmaxf(fabsf(U2.m2), fabsf(U2.m3)))));
+                const float4 L2 = f4(mmul(Mi, Ln)), U2 = f4(mmul(Mi, Un));
+                N[3 * k] = L2;
+                N[3 * k + 1] = U2;
+                N[3 * k + 2] = make_float4(fmaf(Mi.m0, y0, Mi.m1 * y1), fmaf(Mi.m2, y0, Mi.m3 * y1), 0.0f, 0.0f);
+                if (p.final_step) lmax = fmaxf(lmax, fmaxf(amax4(L2), amax4(U2)));
             }
         }
         cur ^= 1;
@@ -298,7 +331,7 @@ mp_pass_kernel(MpPassArgs p)
         }
     }
 
-    const float* S = fsm + cur * 10 * TRm;
+    const float4* S = fsm + cur * 3 * TRm;
     if (p.final_step) {
         // X = Y: write the correction rows and the system's |dx| maximum
         float lmax = 0.0f;
@@ -307,10 +340,10 @@ mp_pass_kernel(MpPassArgs p)
             if (k < TR) {
                 const int64_t kb = r + k * p.G;                 // block row within the system
                 const int64_t i0 = 2 * kb;
-                const float x0 = S[8 * TRm + k], x1 = S[9 * TRm + k];
-                p.dx[j * p.n + i0] = x0;
-                lmax = fmaxf(lmax, fabsf(x0));
-                if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = x1; lmax = fmaxf(lmax, fabsf(x1)); }
+                const float4 xv = S[3 * k + 2];
+                p.dx[j * p.n + i0] = xv.x;
+                lmax = fmaxf(lmax, fabsf(xv.x));
+                if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = xv.y; lmax = fmaxf(lmax, fabsf(xv.y)); }
             }
         }
         lmax = warp_max(lmax);
@@ -322,13 +355,11 @@ mp_pass_kernel(MpPassArgs p)
             const int64_t t = t0 + k;
             if (k < TR && t >= wlo && t < whi) {
                 const int64_t gi = g0 + t * p.G;
-                for (int u = 0; u < 8; u++) {
-                    const float v = S[u * TRm + k];
-                    p.dstLU[u][gi] = v;
-                    lmax = fmaxf(lmax, fabsf(v));
-                }
-                p.dstY[0][gi] = S[8 * TRm + k];
-                p.dstY[1][gi] = S[9 * TRm + k];
+                const float4 Lv = S[3 * k], Uv = S[3 * k + 1], yv = S[3 * k + 2];
+                p.dstLU[2 * gi] = Lv;
+                p.dstLU[2 * gi + 1] = Uv;
+                p.dstY[gi] = make_float2(yv.x, yv.y);
+                lmax = fmaxf(lmax, fmaxf(amax4(Lv), amax4(Uv)));
             }
         }
         lmax = warp_max(lmax);
@@ -336,22 +367,34 @@ mp_pass_kernel(MpPassArgs p)
     }
 }
 
+template <int RPT>
+__global__ void __launch_bounds__(kMpThreads)
+mp_pass_kernel(MpPassArgs p)
+{
+    extern __shared__ float4 fsm[];
+    __shared__ unsigned s_max[2];
+    // grid-stride over the items, so that a pass whose systems are all
+    // finished costs a few hundred CTAs, not one CTA per item
+    const int64_t items = p.m * p.G * p.nwin;
+    for (int64_t blk = blockIdx.x; blk < items; blk += gridDim.x) {
+        const int64_t item = blk / p.nwin;
+        const int64_t w = blk - item * p.nwin;
+        const int64_t j = item / p.G;
+        const int64_t r = item - j * p.G;
+        if (p.fin[j]) continue;
+        // a system whose couplings vanished in an earlier pass is already decoupled
+        if (p.trunc_in && __uint_as_float(p.trunc_in[j]) < kTrunc) mp_copy_item(p, j, r, w);
+        else mp_pass_item<RPT>(p, j, r, w, fsm, s_max);
+        __syncthreads();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // refinement: x += dx (FP64), decide, and r = y - A x for the next sweep
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kMpThreads)
-mp_update_kernel(MpArgs p)
+__device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64_t tile, double* sx, float* s_red)
 {
-    __shared__ double sx[kMpTile + 4];
-    __shared__ float s_red[kMpThreads / 32];
-    const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
-    const int64_t j = blockIdx.x / tiles;
-    const int64_t tile = blockIdx.x - j * tiles;
     const int s = p.sweep;
-    // finished in an earlier sweep?  (fin is written by this kernel's tile-0 CTA
-    // for the current sweep; the other tiles of the system must still run)
-    const int f = p.fin[j];
-    if (f != 0 && f <= s) return;
     const int tid = threadIdx.x;
     const int64_t n = p.n;
 
@@ -364,11 +407,18 @@ mp_update_kernel(MpArgs p)
         const float nxp = __uint_as_float(p.nx[(int64_t)(s - 1) * p.m + j]);
         if (nd == 0.0f) { done = true; est = 0.0f; }
         else if (ndp > 0.0f) {
-            // remaining error after this correction ~ sum_k rho^k |dx| = rho/(1-rho) |dx|;
-            // a factor 2 covers the drift of rho between sweeps
+            // Two ways to be done.  (1) The correction itself is below tol/2:
+            // x_{s-1} was off by about |dx_s|, and applying dx_s leaves at most
+            // that much (this also ends refinement that has reached the FP64
+            // rounding floor, where dx is noise and no longer contracts).
+            // (2) The corrections contract (rho < 0.5): the error left after
+            // dx_s is ~ sum_k rho^k |dx_s| = rho/(1-rho)|dx_s|, doubled for the
+            // drift of rho between sweeps.
+            const float rel = nd / fmaxf(nxp, FLT_MIN);
             const float rho = nd / ndp;
-            est = rho < 0.5f ? 2.0f * rho / (1.0f - rho) * nd / fmaxf(nxp, FLT_MIN) : 1.0f;
-            done = rho < 0.5f && est <= p.tol;
+            const float contr = rho < 0.5f ? 2.0f * rho / (1.0f - rho) * rel : rel;
+            est = fminf(rel, contr);
+            done = rel <= 0.5f * p.tol || (rho < 0.5f && contr <= p.tol);
         }
     }
     const bool last = done || s == p.max_sweeps - 1;
@@ -378,9 +428,12 @@ mp_update_kernel(MpArgs p)
     const int64_t t0 = tile * kMpTile;
     const int64_t t1 = min(t0 + kMpTile, n);
     const int64_t h0 = max(t0 - 2, (int64_t)0), h1 = min(t1 + 2, n);
+    // x_{s-1} comes from the other ping-pong buffer: neighbouring tiles read
+    // their halo rows from it while this tile writes x_s
+    const double* __restrict__ xprev = p.X[(s + 1) & 1];
     for (int64_t i = h0 + tid; i < h1; i += blockDim.x) {
         const double dxi = f2d(p.dx[j * n + i]);
-        sx[i - t0 + 2] = s == 0 ? dxi : __dadd_rn(p.X[j * n + i], dxi);
+        sx[i - t0 + 2] = s == 0 ? dxi : __dadd_rn(xprev[j * n + i], dxi);
     }
     __syncthreads();
 
@@ -389,7 +442,8 @@ mp_update_kernel(MpArgs p)
     for (int64_t i = t0 + tid; i < t1; i += blockDim.x) {
         const double xi = sx[i - t0 + 2];
         if (to_user) p.y[ybase + i * p.rs] = xi;
-        else p.X[j * n + i] = xi;
+        else if (last) p.Xout[j * n + i] = xi;
+        else p.X[s & 1][j * n + i] = xi;
         xmax = fmaxf(xmax, fabsf(d2f_scaled(xi, 0)));     // |x| in FP32: it only feeds the estimate
     }
     xmax = warp_max(xmax);
@@ -429,8 +483,24 @@ mp_update_kernel(MpArgs p)
         }
         const M2 Mi = minv(B.D);
         const int64_t q = j * nb + kb;
-        p.R[q] = fmaf(Mi.m0, rf[0], Mi.m1 * rf[1]);
-        p.R[T + q] = fmaf(Mi.m2, rf[0], Mi.m3 * rf[1]);
+        p.R[q] = make_float2(fmaf(Mi.m0, rf[0], Mi.m1 * rf[1]), fmaf(Mi.m2, rf[0], Mi.m3 * rf[1]));
+    }
+}
+
+__global__ void __launch_bounds__(kMpThreads)
+mp_update_kernel(MpArgs p)
+{
+    __shared__ double sx[kMpTile + 4];
+    __shared__ float s_red[kMpThreads / 32];
+    const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
+    for (int64_t blk = blockIdx.x; blk < p.m * tiles; blk += gridDim.x) {
+        const int64_t j = blk / tiles;
+        const int64_t tile = blk - j * tiles;
+        // finished in an earlier sweep?  (fin is written during this kernel by
+        // the tile-0 CTA for the current sweep; the other tiles must still run)
+        const int f = p.fin[j];
+        if (f == 0 || f > p.sweep) mp_update_tile(p, j, tile, sx, s_red);
+        __syncthreads();
     }
 }
 
@@ -504,10 +574,11 @@ resid_norm_kernel(const double* __restrict__ a, const double* __restrict__ b, co
 template <int RPT>
 cudaError_t launch_mp_pass_rpt(const MpPassArgs& p, int threads, int64_t blocks, cudaStream_t s)
 {
-    const size_t smem = (size_t)20 * p.TRmax * sizeof(float);
+    const size_t smem = (size_t)6 * p.TRmax * sizeof(float4);
     cudaError_t e = cudaFuncSetAttribute(mp_pass_kernel<RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(20 * kMpMaxRows * sizeof(float)));
+                                         (int)(6 * kMpMaxRows * sizeof(float4)));
     if (e != cudaSuccess) return e;
+    blocks = std::min<int64_t>(blocks, mp_grid_cap((const void*)mp_pass_kernel<RPT>, threads, smem));
     mp_pass_kernel<RPT><<<(unsigned)blocks, threads, smem, s>>>(p);
     count_launch();
     return cudaGetLastError();
@@ -530,9 +601,9 @@ cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s)
     int threads = kMpThreads;
     if (p.TRmax < threads) threads = std::max(32, (p.TRmax + 31) / 32 * 32);
     const int rpt = (p.TRmax + threads - 1) / threads;
-    const int64_t blocks = p.m * p.G * p.nwin;
-    if (blocks <= 0) return cudaSuccess;
-    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    const int64_t items = p.m * p.G * p.nwin;
+    if (items <= 0) return cudaSuccess;
+    const int64_t blocks = items;
     if (rpt <= 1) return launch_mp_pass_rpt<1>(p, threads, blocks, s);
     if (rpt <= 2) return launch_mp_pass_rpt<2>(p, threads, blocks, s);
     if (rpt <= 4) return launch_mp_pass_rpt<4>(p, threads, blocks, s);
@@ -543,8 +614,7 @@ cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s)
 cudaError_t launch_mp_update(const MpArgs& p, cudaStream_t s)
 {
     const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
-    const int64_t blocks = p.m * tiles;
-    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    const int64_t blocks = std::min<int64_t>(p.m * tiles, mp_grid_cap((const void*)mp_update_kernel, kMpThreads, 0));
     mp_update_kernel<<<(unsigned)blocks, kMpThreads, 0, s>>>(p);
     count_launch();
     return cudaGetLastError();

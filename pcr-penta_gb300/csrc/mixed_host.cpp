@@ -42,7 +42,7 @@ MpPlan mp_plan(int64_t nb, const pcrp_opts* o)
 }
 
 struct MpLayout {
-    size_t S0, R, P0, P1, dx, X, ndx, nx, fin, status, est, trunc, rbuf, rn, total;
+    size_t S0, R, P0, P1, dx, X0, X1, Xout, ndx, nx, fin, status, est, trunc, rbuf, rn, total;
 };
 
 MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool info)
@@ -51,12 +51,14 @@ MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool 
     MpLayout L{};
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
-    L.S0 = take(8 * T * sizeof(float));
-    L.R = take(2 * T * sizeof(float));
-    L.P0 = pl.s1 > 0 ? take(10 * T * sizeof(float)) : 0;
-    L.P1 = pl.npass > 1 ? take(10 * T * sizeof(float)) : 0;
+    L.S0 = take(2 * T * sizeof(float4));
+    L.R = take(T * sizeof(float2));
+    L.P0 = pl.s1 > 0 ? take(2 * T * sizeof(float4) + T * sizeof(float2)) : 0;
+    L.P1 = pl.npass > 1 ? take(2 * T * sizeof(float4) + T * sizeof(float2)) : 0;
     L.dx = take((size_t)m * n * sizeof(float));
-    L.X = take((size_t)m * n * sizeof(double));
+    L.X0 = take((size_t)m * n * sizeof(double));
+    L.X1 = take((size_t)m * n * sizeof(double));
+    L.Xout = info ? take((size_t)m * n * sizeof(double)) : 0;
     L.ndx = take((size_t)(max_sweeps + 1) * m * sizeof(unsigned));
     L.nx = take((size_t)(max_sweeps + 1) * m * sizeof(unsigned));
     L.fin = take(m * sizeof(int));
@@ -100,8 +102,12 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     MpArgs A{};
     A.a = a; A.b = b; A.c = c; A.d = d; A.e = e; A.y = y;
     A.m = m; A.n = n; A.ss = ss; A.rs = rs;
-    A.S0 = F(WL.S0); A.R = F(WL.R); A.dx = F(WL.dx);
-    A.X = reinterpret_cast<double*>(base + WL.X);
+    A.S0 = reinterpret_cast<float4*>(base + WL.S0);
+    A.R = reinterpret_cast<float2*>(base + WL.R);
+    A.dx = F(WL.dx);
+    A.X[0] = reinterpret_cast<double*>(base + WL.X0);
+    A.X[1] = reinterpret_cast<double*>(base + WL.X1);
+    A.Xout = keep_x ? reinterpret_cast<double*>(base + WL.Xout) : nullptr;
     A.ndx = U(WL.ndx); A.nx = U(WL.nx);
     A.fin = reinterpret_cast<int*>(base + WL.fin);
     A.status = reinterpret_cast<int*>(base + WL.status);
@@ -115,8 +121,7 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     for (int s = 0; s < max_sweeps; s++) {
         // FP32 block-PCR solve of the normalised system with rhs R
         MpPassArgs p{};
-        for (int u = 0; u < 8; u++) p.srcLU[u] = A.S0 + u * T;
-        p.srcY[0] = A.R; p.srcY[1] = A.R + T;
+        p.srcLU = A.S0; p.srcY = A.R;
         p.dx = A.dx; p.fin = A.fin; p.ndx = A.ndx;
         p.m = m; p.n = n; p.nb = nb; p.G = 1; p.sweep = s;
         int done = 0, pass = 0;
@@ -125,9 +130,9 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
             const int H = (1 << K) - 1;
             int Lw = std::max(1, pl.cap - 2 * H);
             const int64_t nrmax = cdiv(nb, p.G);
-            float* D = P[pass & 1];
-            for (int u = 0; u < 8; u++) p.dstLU[u] = D + u * T;
-            p.dstY[0] = D + 8 * T; p.dstY[1] = D + 9 * T;
+            char* D = reinterpret_cast<char*>(P[pass & 1]);
+            p.dstLU = reinterpret_cast<float4*>(D);
+            p.dstY = reinterpret_cast<float2*>(D + 2 * T * sizeof(float4));
             p.K = K; p.H = H; p.L = Lw; p.final_step = 0;
             p.nwin = cdiv(nrmax, Lw);
             p.TRmax = (int)std::min<int64_t>(Lw + 2 * H, nrmax);
@@ -135,8 +140,7 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
             p.trunc_out = A.trunc + pass * m;
             ce = launch_mp_pass(p, st);
             if (ce != cudaSuccess) return cuda_error(ce, "mixed global pass launch");
-            for (int u = 0; u < 8; u++) p.srcLU[u] = D + u * T;
-            p.srcY[0] = D + 8 * T; p.srcY[1] = D + 9 * T;
+            p.srcLU = p.dstLU; p.srcY = p.dstY;
             p.G <<= K; done += K; pass++;
         }
         const int64_t nrmax = cdiv(nb, p.G);
@@ -166,6 +170,7 @@ extern "C" pcrp_status pcrp_solve_mixed(const double* a, const double* b, const 
                                         pcrp_mixed_info* info)
 {
     const char* who = "pcrp_solve_mixed";
+    NvtxRange nv(who);
     if (m < 0 || n < 0) return set_error(PCRP_EINVAL, "%s: negative size", who);
     if (!valid_layout(layout)) return set_error(PCRP_EINVAL, "%s: bad layout %d", who, layout);
     if (info) std::memset(info, 0, sizeof *info);
@@ -201,9 +206,9 @@ extern "C" pcrp_status pcrp_solve_mixed(const double* a, const double* b, const 
     unsigned* rn = U(WL.rn);
     ce = cudaMemsetAsync(rn, 0, 3 * m * sizeof(unsigned), st);
     if (ce != cudaSuccess) return cuda_error(ce, "cudaMemsetAsync");
-    ce = launch_residual(a, b, c, d, e, y, A.X, rb, m, n, A.ss, A.rs, n, 1, st);
-    if (ce == cudaSuccess) ce = launch_resid_norm(a, b, c, d, e, A.X, rb, m, n, A.ss, A.rs, rn, rn + m, rn + 2 * m, st);
-    if (ce == cudaSuccess) ce = launch_copy_out(A.X, y, m, n, A.ss, A.rs, st);
+    ce = launch_residual(a, b, c, d, e, y, A.Xout, rb, m, n, A.ss, A.rs, n, 1, st);
+    if (ce == cudaSuccess) ce = launch_resid_norm(a, b, c, d, e, A.Xout, rb, m, n, A.ss, A.rs, rn, rn + m, rn + 2 * m, st);
+    if (ce == cudaSuccess) ce = launch_copy_out(A.Xout, y, m, n, A.ss, A.rs, st);
     if (ce != cudaSuccess) return cuda_error(ce, "mixed report launch");
     std::vector<unsigned> norms(3 * m);
     ce = cudaMemcpyAsync(norms.data(), rn, 3 * m * sizeof(unsigned), cudaMemcpyDeviceToHost, st);

@@ -6,7 +6,7 @@
 namespace pcrp {
 
 constexpr int kMpTile = 1024;      // rows per CTA of the refinement kernel (even)
-constexpr int kMpMaxRows = 2048;   // block rows per CTA of the FP32 PCR kernel (20 floats each)
+constexpr int kMpMaxRows = 2048;   // block rows per CTA of the FP32 PCR kernel (2 x 48 bytes each)
 constexpr int kMpMaxPasses = 24;   // global FP32 passes per solve
 
 // Whole-batch arguments (prep and refinement kernels).
@@ -14,10 +14,11 @@ struct MpArgs {
     const double *a, *b, *c, *d, *e;   // caller bands, layout (ss, rs)
     double* y;                          // caller rhs in, solution out
     int64_t m, n, ss, rs;
-    float* S0;                          // level-0 normalised L,U: 8 arrays of m*nb
-    float* R;                           // normalised rhs Y: 2 arrays of m*nb
+    float4* S0;                         // level-0 normalised L,U: [2*q] = L, [2*q+1] = U, q < m*nb
+    float2* R;                          // normalised rhs Y of block row q
     float* dx;                          // FP32 correction, m*n (contiguous)
-    double* X;                          // FP64 iterate, m*n (contiguous)
+    double* X[2];                       // FP64 iterates, m*n each (contiguous): sweep s writes X[s&1]
+    double* Xout;                       // final iterate when the caller asked for a report (keep_x)
     unsigned* ndx;                      // [(max_sweeps+1) x m] max |dx| per sweep (float bits)
     unsigned* nx;                       // [(max_sweeps+1) x m] max |x| per sweep
     int* fin;                           // per system: 0 running, else the sweep it finished in, plus 1
@@ -30,10 +31,10 @@ struct MpArgs {
 
 // One FP32 block-PCR pass.
 struct MpPassArgs {
-    const float* srcLU[8];
-    const float* srcY[2];
-    float* dstLU[8];
-    float* dstY[2];
+    const float4* srcLU;                // [2*q] = L, [2*q+1] = U of block row q
+    const float2* srcY;
+    float4* dstLU;
+    float2* dstY;
     float* dx;
     const int* fin;                     // systems with fin != 0 are finished: skip them
     unsigned* ndx;                      // final pass: max |dx| of this sweep

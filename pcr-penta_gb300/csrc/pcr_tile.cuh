@@ -11,6 +11,9 @@ __device__ __forceinline__ double mul(double x, double y) { return __dmul_rn(x, 
 __device__ __forceinline__ double add(double x, double y) { return __dadd_rn(x, y); }
 __device__ __forceinline__ double sub(double x, double y) { return __dsub_rn(x, y); }
 __device__ __forceinline__ double dvd(double x, double y) { return __ddiv_rn(x, y); }
+// x != 0.0 evaluated on the integer pipe (same truth table: false for +-0,
+// true for everything else including NaN), sparing the FP64 pipe a compare
+__device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) << 1) != 0; }
 
 constexpr int kMaxThreads = 256;
 constexpr int kSmemArrays = 14;   // 6 state + 6 T coefficients + 2 T multipliers
@@ -103,8 +106,8 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                                      eL = se[k - dl], yL = sy[k - dl];
                         const double aR = sa[k + dl], bR = sb[k + dl], cR = sc[k + dl], dR = sd[k + dl],
                                      eR = se[k + dl], yR = sy[k + dl];
-                        if (t - 2 * dl >= 0 && bL != 0.0) al1 = dvd(-am, bL);
-                        if (t + 2 * dl <= nr - 1 && dR != 0.0) al2 = dvd(-em, dR);
+                        if (t - 2 * dl >= 0 && nz(bL)) al1 = dvd(-am, bL);
+                        if (t + 2 * dl <= nr - 1 && nz(dR)) al2 = dvd(-em, dR);
                         aT = mul(al1, aL);
                         bT = add(add(mul(al1, cL), bm), mul(al2, aR));
                         cT = add(add(mul(al1, dL), cm), mul(al2, bR));
@@ -115,7 +118,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                         const double aR = sa[k + dl], bR = sb[k + dl], cR = sc[k + dl], dR = sd[k + dl],
                                      eR = se[k + dl], yR = sy[k + dl];
                         (void)aR;
-                        if (t + 2 * dl <= nr - 1 && dR != 0.0) al2 = dvd(-em, dR);
+                        if (t + 2 * dl <= nr - 1 && nz(dR)) al2 = dvd(-em, dR);
                         aT = 0.0; bT = 0.0;
                         cT = add(cm, mul(al2, bR));
                         dT = add(dm, mul(al2, cR));
@@ -124,7 +127,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                     } else {               // row m+d outside: kernel.cu:108-117
                         const double aL = sa[k - dl], bL = sb[k - dl], cL = sc[k - dl], dL = sd[k - dl],
                                      yL = sy[k - dl];
-                        if (t - 2 * dl >= 0 && bL != 0.0) al1 = dvd(-am, bL);
+                        if (t - 2 * dl >= 0 && nz(bL)) al1 = dvd(-am, bL);
                         aT = mul(al1, aL);
                         bT = add(mul(al1, cL), bm);
                         cT = add(mul(al1, dL), cm);
@@ -154,13 +157,13 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                 double b2 = 0.0, c2 = 0.0, d2 = 0.0, e2 = 0.0, k2 = 0.0, f2 = a2pre;
                 if (hasL) {                // kernel.cu:120-125
                     const double cTL = Tc[k - dl];
-                    if (cTL != 0.0) f1 = dvd(bi, cTL);
+                    if (nz(cTL)) f1 = dvd(bi, cTL);
                     a1 = mul(f1, Ta[k - dl]); b1 = mul(f1, Tb[k - dl]); c1 = mul(f1, Td[k - dl]);
                     d1 = mul(f1, Te[k - dl]); k1 = mul(f1, Tk[k - dl]);
                 }
                 if (hasR) {                // kernel.cu:127-132
                     const double cTR = Tc[k + dl];
-                    if (cTR != 0.0) f2 = dvd(di, cTR);
+                    if (nz(cTR)) f2 = dvd(di, cTR);
                     c2 = mul(f2, Tb[k + dl]); b2 = mul(f2, Ta[k + dl]); d2 = mul(f2, Td[k + dl]);
                     e2 = mul(f2, Te[k + dl]); k2 = mul(f2, Tk[k + dl]);
                 }

@@ -5,9 +5,20 @@
 #include <cstddef>
 #include <cuda_runtime.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "pcrp.h"
 
 namespace pcrp {
+
+// NVTX range around an entry point (visible in Nsight timelines; no cost when
+// no tool is attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Six band/state arrays of a pentadiagonal batch: a b c d e y.  The faithful
 // PCR state adds the two per-row multipliers that persist across strides

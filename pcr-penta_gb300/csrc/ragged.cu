@@ -359,6 +359,7 @@ extern "C" pcrp_status pcrp_solve_ragged(const double* a, const double* b, const
                                          int64_t max_rows, int32_t mode, double tol, int32_t max_sweeps,
                                          const pcrp_opts* opts, pcrp_stream stream)
 {
+    NvtxRange nv("pcrp_solve_ragged");
     if (nsys < 0 || max_rows < 0) return set_error(PCRP_EINVAL, "pcrp_solve_ragged: negative size");
     if (mode != 0 && mode != 1) return set_error(PCRP_EINVAL, "pcrp_solve_ragged: mode %d (0 FP64, 1 mixed)", mode);
     if (nsys == 0 || max_rows == 0) return PCRP_OK;

@@ -75,6 +75,7 @@ _SIGS = {
     "pcrp_solve_f64_noalloc": [_vp] * 6 + [_i64, _i64, _i32, _vp],
     "pcrp_solve_mixed": [_vp] * 6 + [_i64, _i64, _i32, ctypes.c_double, _i32, _vp, _vp, _vp],
     "pcrp_residual_f64": [_vp] * 8 + [_i64, _i64, _i32, _vp],
+    "pcrp_solve_host": [_vp] * 6 + [_i64, _i64, _i32, _i32, ctypes.c_double, _i32, _vp, _vp],
     "pcrp_solve_ragged": [_vp] * 6 + [_vp, _i64, _i64, _i32, ctypes.c_double, _i32, _vp, _vp],
     "pcrp_workspace_size": [_i64, _i64, _i32, _i32, _vp, ctypes.POINTER(ctypes.c_size_t)],
     "pcrp_release_workspace": [],
@@ -183,6 +184,28 @@ def solve_mixed(a, b, c, d, e, y, m: int, n: int, layout: int = CONTIGUOUS, tol:
                                 _opts(opts), _stream(stream), ctypes.byref(info) if info is not None else None)
     _check(rc, "pcrp_solve_mixed")
     return info
+
+
+def _host_ptr(x) -> int:
+    if hasattr(x, "ctypes"):
+        if not x.flags.c_contiguous:
+            raise ValueError("expected a contiguous array")
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        if x.is_cuda:
+            raise ValueError("expected a host tensor")
+        return x.data_ptr()
+    return int(x)
+
+
+def solve_host(a, b, c, d, e, y, m: int, n: int, layout: int = CONTIGUOUS, precision: int = 0,
+               tol: float = 1e-12, max_sweeps: int = 8, opts: Optional[Opts] = None, stream=None) -> None:
+    """Solve a batch held in host memory (numpy arrays or CPU tensors, float64):
+    chunks stream through the GPU with copies overlapping solves (pcrp_solve_host).
+    Asynchronous on `stream`; synchronise before reading y."""
+    rc = lib().pcrp_solve_host(*[_host_ptr(v) for v in (a, b, c, d, e, y)], m, n, layout, precision, tol,
+                               max_sweeps, _opts(opts), _stream(stream))
+    _check(rc, "pcrp_solve_host")
 
 
 def residual_f64(a, b, c, d, e, y, x, r, m: int, n: int, layout: int = CONTIGUOUS, stream=None) -> None:

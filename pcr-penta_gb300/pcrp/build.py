@@ -16,6 +16,8 @@ CSRC = os.path.join(PKG_ROOT, "csrc")
 INCLUDE = os.path.join(REPO_ROOT, "include")
 BUILD_DIR = os.path.join(PKG_ROOT, "_build")
 LIB_PATH = os.path.join(PKG_ROOT, "libpcrp.so")
+CMP_SRC = os.path.join(PKG_ROOT, "compare", "cusparse_gpsv.cpp")
+CMP_LIB = os.path.join(PKG_ROOT, "compare", "libpcrp_cmp.so")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -61,7 +63,19 @@ def build(verbose: bool = False, force: bool = False) -> str:
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"nvcc link failed:\n{res.stdout}\n{res.stderr}")
+    build_compare()
     return LIB_PATH
+
+
+def build_compare() -> str:
+    """The cuSPARSE comparison library (benchmark only, not part of libpcrp)."""
+    if not os.path.exists(CMP_LIB) or os.path.getmtime(CMP_LIB) < os.path.getmtime(CMP_SRC):
+        cmd = [NVCC] + ARCH + ["-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", CMP_SRC,
+                               "-o", CMP_LIB, "-lcusparse"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"nvcc failed on the cuSPARSE comparison:\n{res.stdout}\n{res.stderr}")
+    return CMP_LIB
 
 
 if __name__ == "__main__":

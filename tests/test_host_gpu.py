@@ -1,0 +1,34 @@
+"""pcrp_solve_host: batches in host memory streamed through the GPU in chunks.
+FP64 results must equal the device entry point bit for bit; mixed results
+must meet the 1e-12 bar."""
+import numpy as np
+import pytest
+
+import oracle as O
+import pcrp
+from helpers import assert_bitexact, dd_bands, gpu_f64, to_layout
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("m,n,layout", [(1, 100, 0), (13, 700, 0), (13, 700, 1), (9, 5000, 0), (9, 5000, 1), (64, 512, 0)])
+def test_host_f64_equals_device(cuda, m, n, layout):
+    import torch
+    arrs = to_layout(dd_bands(np.random.default_rng(m * n), m, n, garbage=True), m, n, layout)
+    xd, _ = gpu_f64(arrs, m, n, layout)
+    h = [torch.from_numpy(v.copy()).pin_memory() for v in arrs]
+    pcrp.solve_host(*h, m, n, layout, precision=0)
+    torch.cuda.synchronize()
+    assert_bitexact(h[5].numpy(), xd, f"host m={m} n={n} layout={layout}")
+    for u, v in zip(h[:5], arrs[:5]):
+        assert np.array_equal(u.numpy(), v)
+
+
+def test_host_mixed_meets_tolerance_pageable(cuda):
+    import torch
+    m, n = 11, 3000
+    arrs = dd_bands(np.random.default_rng(1), m, n)
+    h = [v.copy() for v in arrs]                      # pageable numpy memory
+    pcrp.solve_host(*h, m, n, precision=1)
+    torch.cuda.synchronize()
+    assert O.fwd_err(h[5], O.ge(*arrs, m, n), m, n) <= 1e-12

@@ -59,19 +59,18 @@ def test_mixed_forced_global_passes(cuda, opts):
 
 def test_mixed_ill_conditioned_adi(cuda):
     """ADI at n = 65536: entries reach ~1e6 against a unit dominance margin
-    (condition ~1e6).  FP32 corrections contract slowly (rho ~ 1e-2) and the
-    FP64 residual itself limits the attainable accuracy to ~cond*eps, so a
-    1e-12 target is out of reach: the solver must say so (PCRP_ENOCONV) rather
-    than claim it, and it must converge to a 1e-9 target, agreeing with FP64
-    elimination (itself only good to ~cond*eps) to that level."""
+    (condition ~1e6), so FP32 corrections contract slowly (rho ~ 1e-2) and take
+    several sweeps; the refinement must still get there.  FP64 elimination is
+    itself only good to ~cond*eps here, so it is refined with long-double
+    residuals to give the reference answer."""
     m, n = 4, 65536
     arrs = pcrp.generate(pcrp.GEN_ADI, 17, m, n)
-    with pytest.raises(pcrp.PcrpError) as ei:
-        run_mixed(arrs, m, n, max_sweeps=12)
-    assert ei.value.status == 5
-    x, info, _ = run_mixed(arrs, m, n, tol=1e-9, max_sweeps=16)
+    x, info, _ = run_mixed(arrs, m, n, max_sweeps=16)
     assert info.converged == 1 and info.sweeps >= 3
-    assert O.fwd_err(x, O.ge(*arrs, m, n), m, n) <= 1e-9
+    xt = O.ge(*arrs, m, n)
+    for _ in range(3):
+        xt = xt + O.ge(*arrs[:5], O.residual(*arrs, xt, m, n), m, n)
+    assert O.fwd_err(x, xt, m, n) <= 1e-11
 
 
 def test_mixed_solves_what_the_reference_algorithm_cannot(cuda):
