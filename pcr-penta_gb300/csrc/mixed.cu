@@ -124,36 +124,60 @@ __device__ __forceinline__ M2 minv(const M2& D) {
     return {D.m3 * r, -D.m1 * r, -D.m2 * r, D.m0 * r};
 }
 
+// The six FP64 values of rows i0 = 2k and i1 = 2k+1 of one system (i1 may be
+// the dummy row n of an odd system).  Contiguous pairs at an even element
+// offset are read as one 16-byte load per array.
+struct PairRow { double a0, a1, b0, b1, c0, c1, d0, d1, e0, e1, y0, y1; };
+
+__device__ __forceinline__ PairRow load_pair(const MpArgs& p, int64_t base, int64_t i0)
+{
+    PairRow P;
+    const int64_t n = p.n, rs = p.rs;
+    const int64_t g0 = base + i0 * rs;
+    if (p.vec && rs == 1 && ((g0 & 1) == 0) && i0 + 1 < n) {
+        const double2 a = *reinterpret_cast<const double2*>(p.a + g0);
+        const double2 b = *reinterpret_cast<const double2*>(p.b + g0);
+        const double2 c = *reinterpret_cast<const double2*>(p.c + g0);
+        const double2 d = *reinterpret_cast<const double2*>(p.d + g0);
+        const double2 e = *reinterpret_cast<const double2*>(p.e + g0);
+        const double2 y = *reinterpret_cast<const double2*>(p.y + g0);
+        P = {a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x, e.y, y.x, y.y};
+    } else {
+        P.a0 = p.a[g0]; P.b0 = p.b[g0]; P.c0 = p.c[g0]; P.d0 = p.d[g0]; P.e0 = p.e[g0]; P.y0 = p.y[g0];
+        if (i0 + 1 < n) {
+            const int64_t g1 = g0 + rs;
+            P.a1 = p.a[g1]; P.b1 = p.b[g1]; P.c1 = p.c[g1]; P.d1 = p.d[g1]; P.e1 = p.e[g1]; P.y1 = p.y[g1];
+        } else {
+            P.a1 = 0.0; P.b1 = 0.0; P.c1 = 1.0; P.d1 = 0.0; P.e1 = 0.0; P.y1 = 0.0;
+        }
+    }
+    return P;
+}
+
 // The FP32 row-scaled diagonal block and couplings of block row k (rows
 // i0 = 2k, i1 = 2k+1) of a system with n rows.  Row i1 = n (odd n) is a
-// dummy identity row.  Bands are read through (base, rs).
+// dummy identity row.  Out-of-range band slots are never read as values.
 struct BlockRow { M2 D, L, U; int sh0, sh1; };
 
-__device__ __forceinline__ BlockRow load_block(const double* __restrict__ a, const double* __restrict__ b,
-                                               const double* __restrict__ c, const double* __restrict__ d,
-                                               const double* __restrict__ e, int64_t base, int64_t rs,
-                                               int64_t i0, int64_t n) {
+__device__ __forceinline__ BlockRow block_of(const PairRow& P, int64_t i0, int64_t n)
+{
     BlockRow B;
     const int64_t i1 = i0 + 1;
-    const int64_t g0 = base + i0 * rs, g1 = base + i1 * rs;
-    const double c0 = c[g0];
-    B.sh0 = d_exponent(c0);
-    const float a0 = i0 >= 2 ? d2f_scaled(a[g0], B.sh0) : 0.0f;
-    const float b0 = i0 >= 1 ? d2f_scaled(b[g0], B.sh0) : 0.0f;
-    const float d0 = i0 + 1 < n ? d2f_scaled(d[g0], B.sh0) : 0.0f;
-    const float e0 = i0 + 2 < n ? d2f_scaled(e[g0], B.sh0) : 0.0f;
-    const float cf0 = d2f_scaled(c0, B.sh0);
+    B.sh0 = d_exponent(P.c0);
+    const float a0 = i0 >= 2 ? d2f_scaled(P.a0, B.sh0) : 0.0f;
+    const float b0 = i0 >= 1 ? d2f_scaled(P.b0, B.sh0) : 0.0f;
+    const float d0 = i0 + 1 < n ? d2f_scaled(P.d0, B.sh0) : 0.0f;
+    const float e0 = i0 + 2 < n ? d2f_scaled(P.e0, B.sh0) : 0.0f;
+    const float cf0 = d2f_scaled(P.c0, B.sh0);
     float a1 = 0.0f, b1 = 0.0f, cf1 = 1.0f, d1 = 0.0f, e1 = 0.0f;
     B.sh1 = 0;
     if (i1 < n) {
-        const double c1 = c[g1];
-        B.sh1 = d_exponent(c1);
-        a1 = d2f_scaled(a[g1], B.sh1);                         // i1 >= 1, a is in range for i1 >= 2
-        if (i1 < 2) a1 = 0.0f;
-        b1 = d2f_scaled(b[g1], B.sh1);
-        cf1 = d2f_scaled(c1, B.sh1);
-        d1 = i1 + 1 < n ? d2f_scaled(d[g1], B.sh1) : 0.0f;
-        e1 = i1 + 2 < n ? d2f_scaled(e[g1], B.sh1) : 0.0f;
+        B.sh1 = d_exponent(P.c1);
+        a1 = i1 >= 2 ? d2f_scaled(P.a1, B.sh1) : 0.0f;
+        b1 = d2f_scaled(P.b1, B.sh1);
+        cf1 = d2f_scaled(P.c1, B.sh1);
+        d1 = i1 + 1 < n ? d2f_scaled(P.d1, B.sh1) : 0.0f;
+        e1 = i1 + 2 < n ? d2f_scaled(P.e1, B.sh1) : 0.0f;
     }
     B.D = {cf0, d0, b1, cf1};
     B.L = {a0, b0, 0.0f, a1};
@@ -173,11 +197,12 @@ mp_prep_kernel(MpArgs p)
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = q / nb, k = q - j * nb;
         const int64_t base = j * p.ss;
-        const BlockRow B = load_block(p.a, p.b, p.c, p.d, p.e, base, p.rs, 2 * k, p.n);
+        const PairRow P = load_pair(p, base, 2 * k);
+        const BlockRow B = block_of(P, 2 * k, p.n);
         const M2 Mi = minv(B.D);
         const M2 L = mmul(Mi, B.L), U = mmul(Mi, B.U);
-        const float y0 = d2f_scaled(p.y[base + 2 * k * p.rs], B.sh0);
-        const float y1 = 2 * k + 1 < p.n ? d2f_scaled(p.y[base + (2 * k + 1) * p.rs], B.sh1) : 0.0f;
+        const float y0 = d2f_scaled(P.y0, B.sh0);
+        const float y1 = 2 * k + 1 < p.n ? d2f_scaled(P.y1, B.sh1) : 0.0f;
         p.S0[2 * q] = make_float4(L.m0, L.m1, L.m2, L.m3);
         p.S0[2 * q + 1] = make_float4(U.m0, U.m1, U.m2, U.m3);
         p.R[q] = make_float2(fmaf(Mi.m0, y0, Mi.m1 * y1), fmaf(Mi.m2, y0, Mi.m3 * y1));
@@ -466,20 +491,22 @@ __device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64
     const int64_t nb = (n + 1) / 2;
     const int64_t T = p.m * nb;
     for (int64_t kb = t0 / 2 + tid; 2 * kb < t1; kb += blockDim.x) {
-        const BlockRow B = load_block(p.a, p.b, p.c, p.d, p.e, ybase, p.rs, 2 * kb, n);
+        const PairRow P = load_pair(p, ybase, 2 * kb);
+        const BlockRow B = block_of(P, 2 * kb, n);
         float rf[2] = {0.0f, 0.0f};
+#pragma unroll
         for (int h = 0; h < 2; h++) {
             const int64_t i = 2 * kb + h;
-            if (i >= n) break;
-            const int64_t g = ybase + i * p.rs;
-            const int li = (int)(i - t0 + 2);
-            double r = p.y[g];
-            r = fma(-p.c[g], sx[li], r);
-            if (i >= 2) r = fma(-p.a[g], sx[li - 2], r);
-            if (i >= 1) r = fma(-p.b[g], sx[li - 1], r);
-            if (i + 1 < n) r = fma(-p.d[g], sx[li + 1], r);
-            if (i + 2 < n) r = fma(-p.e[g], sx[li + 2], r);
-            rf[h] = d2f_scaled(r, h == 0 ? B.sh0 : B.sh1);
+            if (i < n) {
+                const int li = (int)(i - t0 + 2);
+                double r = h ? P.y1 : P.y0;
+                r = fma(-(h ? P.c1 : P.c0), sx[li], r);
+                if (i >= 2) r = fma(-(h ? P.a1 : P.a0), sx[li - 2], r);
+                if (i >= 1) r = fma(-(h ? P.b1 : P.b0), sx[li - 1], r);
+                if (i + 1 < n) r = fma(-(h ? P.d1 : P.d0), sx[li + 1], r);
+                if (i + 2 < n) r = fma(-(h ? P.e1 : P.e0), sx[li + 2], r);
+                rf[h] = d2f_scaled(r, h == 0 ? B.sh0 : B.sh1);
+            }
         }
         const M2 Mi = minv(B.D);
         const int64_t q = j * nb + kb;

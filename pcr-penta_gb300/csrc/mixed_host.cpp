@@ -113,6 +113,11 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     A.status = reinterpret_cast<int*>(base + WL.status);
     A.est = F(WL.est); A.trunc = U(WL.trunc);
     A.max_sweeps = max_sweeps; A.tol = (float)tol; A.keep_x = keep_x;
+    {
+        const void* ptrs[6] = {a, b, c, d, e, y};
+        A.vec = 1;
+        for (const void* q : ptrs) if (reinterpret_cast<uintptr_t>(q) & 15) A.vec = 0;
+    }
 
     cudaError_t ce = launch_mp_prep(A, st);
     if (ce != cudaSuccess) return cuda_error(ce, "mixed prep launch");

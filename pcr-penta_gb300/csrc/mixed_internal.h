@@ -26,6 +26,7 @@ struct MpArgs {
     float* est;                         // per system: estimated relative forward error
     unsigned* trunc;                    // [kMpMaxPasses x m] max |L|,|U| after each global pass
     int sweep, max_sweeps, keep_x;
+    int vec;                            // 1: all six caller arrays are 16-byte aligned (paired loads allowed)
     float tol;
 };
 

@@ -14,6 +14,10 @@ __device__ __forceinline__ double dvd(double x, double y) { return __ddiv_rn(x, 
 // x != 0.0 evaluated on the integer pipe (same truth table: false for +-0,
 // true for everything else including NaN), sparing the FP64 pipe a compare
 __device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) << 1) != 0; }
+// -x by flipping the sign bit on the integer pipe (bit-identical to unary minus)
+__device__ __forceinline__ double neg(double x) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+}
 
 constexpr int kMaxThreads = 256;
 constexpr int kSmemArrays = 14;   // 6 state + 6 T coefficients + 2 T multipliers
@@ -106,8 +110,8 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                                      eL = se[k - dl], yL = sy[k - dl];
                         const double aR = sa[k + dl], bR = sb[k + dl], cR = sc[k + dl], dR = sd[k + dl],
                                      eR = se[k + dl], yR = sy[k + dl];
-                        if (t - 2 * dl >= 0 && nz(bL)) al1 = dvd(-am, bL);
-                        if (t + 2 * dl <= nr - 1 && nz(dR)) al2 = dvd(-em, dR);
+                        if (t - 2 * dl >= 0 && nz(bL)) al1 = dvd(neg(am), bL);
+                        if (t + 2 * dl <= nr - 1 && nz(dR)) al2 = dvd(neg(em), dR);
                         aT = mul(al1, aL);
                         bT = add(add(mul(al1, cL), bm), mul(al2, aR));
                         cT = add(add(mul(al1, dL), cm), mul(al2, bR));
@@ -118,7 +122,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                         const double aR = sa[k + dl], bR = sb[k + dl], cR = sc[k + dl], dR = sd[k + dl],
                                      eR = se[k + dl], yR = sy[k + dl];
                         (void)aR;
-                        if (t + 2 * dl <= nr - 1 && nz(dR)) al2 = dvd(-em, dR);
+                        if (t + 2 * dl <= nr - 1 && nz(dR)) al2 = dvd(neg(em), dR);
                         aT = 0.0; bT = 0.0;
                         cT = add(cm, mul(al2, bR));
                         dT = add(dm, mul(al2, cR));
@@ -127,7 +131,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                     } else {               // row m+d outside: kernel.cu:108-117
                         const double aL = sa[k - dl], bL = sb[k - dl], cL = sc[k - dl], dL = sd[k - dl],
                                      yL = sy[k - dl];
-                        if (t - 2 * dl >= 0 && nz(bL)) al1 = dvd(-am, bL);
+                        if (t - 2 * dl >= 0 && nz(bL)) al1 = dvd(neg(am), bL);
                         aT = mul(al1, aL);
                         bT = add(mul(al1, cL), bm);
                         cT = add(mul(al1, dL), cm);

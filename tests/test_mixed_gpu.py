@@ -137,3 +137,18 @@ def test_residual_f64_matches_oracle(cuda, layout):
     ro = O.residual(*arrs, x, m, n, layout)
     scale = np.abs(arrs[2]).max() * np.abs(x).max()
     assert np.abs(r - ro).max() <= 8 * np.finfo(float).eps * scale
+
+
+def test_mixed_unaligned_arrays(cuda):
+    """Arrays that start 8 bytes past a 16-byte boundary take the scalar load path."""
+    import torch
+    m, n = 4, 2000
+    arrs = dd_bands(np.random.default_rng(31), m, n)
+    bufs = [torch.empty(m * n + 1, dtype=torch.float64, device=cuda) for _ in range(6)]
+    views = [b[1:] for b in bufs]
+    for v, h in zip(views, arrs):
+        v.copy_(torch.from_numpy(h))
+    assert views[0].data_ptr() % 16 == 8
+    pcrp.solve_mixed(*views, m, n)
+    torch.cuda.synchronize()
+    assert O.fwd_err(views[5].cpu().numpy(), O.ge(*arrs, m, n), m, n) <= TOL
