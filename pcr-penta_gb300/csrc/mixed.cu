@@ -43,8 +43,9 @@ namespace {
 
 constexpr float kTrunc = 1e-10f;
 constexpr int kMpThreads = 256;
-// grid-stride kernels launch about one wave: a sweep whose systems have all
-// finished then costs a few microseconds per kernel
+static_assert(kMpTile % kMpThreads == 0 && kMpThreads % 2 == 0, "refinement tiles: whole rows per thread, pairs in adjacent lanes");
+// CTAs of one wave of a kernel (the pass kernel strides over its items with
+// one wave, so that sweeps of mostly finished systems stay cheap)
 int mp_grid_cap(const void* kernel, int threads, size_t smem)
 {
     int dev = 0, sms = 0, per = 0;
@@ -215,58 +216,30 @@ mp_prep_kernel(MpArgs p)
         for (int64_t q = threadIdx.x; q < (int64_t)(p.max_sweeps + 1) * p.m; q += blockDim.x) {
             p.ndx[q] = 0u; p.nx[q] = 0u;
         }
+        for (int64_t q = threadIdx.x; q < (int64_t)p.max_sweeps * kMpMaxPasses * p.m; q += blockDim.x)
+            p.ndx_pre[q] = 0u;
+        for (int q = threadIdx.x; q <= p.max_sweeps; q += blockDim.x) p.live[q] = (int)p.m;
     }
 }
 
 // ---------------------------------------------------------------------------
 // FP32 block PCR pass (windows + halos at block level G, or whole subsystems)
 // ---------------------------------------------------------------------------
-// Copy of the decoupled rows of a system whose couplings already vanished:
-// X = Y (final: write dx and its maximum) or the rhs carried to the next level
-// (non-final).  Item r of the G items of system j takes a contiguous range of
-// block rows, so the accesses coalesce whatever the gather stride.
-__device__ __forceinline__ void mp_copy_item(const MpPassArgs& p, int64_t j, int64_t r, int64_t w)
-{
-    const int64_t nb = p.nb;
-    const int64_t parts = p.G * p.nwin;
-    const int64_t part = r * p.nwin + w;
-    const int64_t per = (nb + parts - 1) / parts;
-    const int64_t k0 = part * per, k1 = min(k0 + per, nb);
-    float lmax = 0.0f;
-    for (int64_t kb = k0 + threadIdx.x; kb < k1; kb += blockDim.x) {
-        const int64_t q = j * nb + kb;
-        const float2 yv = p.srcY[q];
-        if (p.final_step) {
-            const int64_t i0 = 2 * kb;
-            p.dx[j * p.n + i0] = yv.x;
-            lmax = fmaxf(lmax, fabsf(yv.x));
-            if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = yv.y; lmax = fmaxf(lmax, fabsf(yv.y)); }
-        } else {
-            p.dstY[q] = yv;
-        }
-    }
-    if (p.final_step) {
-        lmax = warp_max(lmax);
-        if ((threadIdx.x & 31) == 0) atomic_max_pos(&p.ndx[(int64_t)p.sweep * p.m + j], lmax);
-    } else if (threadIdx.x == 0 && p.trunc_out && r == 0 && w == 0) {
-        atomicMax(&p.trunc_out[j], p.trunc_in[j]);         // stays below the threshold
-    }
-}
-
-__device__ __forceinline__ float amax4(const float4& v) {
-    return fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
+__device__ __forceinline__ float amaxm(const M2& a) {
+    return fmaxf(fmaxf(fabsf(a.m0), fabsf(a.m1)), fmaxf(fabsf(a.m2), fabsf(a.m3)));
 }
 __device__ __forceinline__ M2 m2(const float4& v) { return {v.x, v.y, v.z, v.w}; }
 __device__ __forceinline__ float4 f4(const M2& a) { return make_float4(a.m0, a.m1, a.m2, a.m3); }
 
-// One window (or whole subsystem) of one FP32 block-PCR pass.  Shared memory
-// holds two buffers of TRmax block rows, each row 3 float4 (L, U, Y + pad):
-// vector accesses, conflict-free at the 48-byte row pitch.
+// One window (or whole subsystem) of one FP32 block-PCR pass.  Each thread
+// keeps the rows it owns (k = tid + q*blockDim) in registers; shared memory
+// holds one copy of the level's rows (L and U as float4 arrays, Y as float2),
+// read for the two neighbours of a row and rewritten after every stride:
+// 80 bytes read and 40 written per row and stride, conflict-free.
 template <int RPT>
 __device__ __forceinline__ void mp_pass_item(const MpPassArgs& p, int64_t j, int64_t r, int64_t w,
-                                             float4* fsm, unsigned* s_max)
+                                             float4* sL, float4* sU, float2* sY, unsigned* s_max)
 {
-    const int TRm = p.TRmax;
     const int64_t nb = p.nb;
     if (r >= nb) return;
     const int64_t nr = (nb - 1 - r) / p.G + 1;
@@ -280,20 +253,23 @@ __device__ __forceinline__ void mp_pass_item(const MpPassArgs& p, int64_t j, int
     const int64_t g0 = j * nb + r;                 // block row of local t = 0
     const int K = p.K;
 
+    M2 Lr[RPT], Ur[RPT];
+    float2 Yr[RPT];
+#pragma unroll
     for (int q = 0; q < RPT; q++) {
         const int k = tid + q * bd;
+        Lr[q] = {0.0f, 0.0f, 0.0f, 0.0f}; Ur[q] = Lr[q]; Yr[q] = make_float2(0.0f, 0.0f);
         if (k < TR) {
             const int64_t gi = g0 + (t0 + k) * p.G;
+            const float4 lv = p.srcLU[2 * gi], uv = p.srcLU[2 * gi + 1];
             const float2 yv = p.srcY[gi];
-            fsm[3 * k] = p.srcLU[2 * gi];
-            fsm[3 * k + 1] = p.srcLU[2 * gi + 1];
-            fsm[3 * k + 2] = make_float4(yv.x, yv.y, 0.0f, 0.0f);
+            sL[k] = lv; sU[k] = uv; sY[k] = yv;
+            Lr[q] = m2(lv); Ur[q] = m2(uv); Yr[q] = yv;
         }
     }
-    if (tid == 0) { s_max[0] = 0u; s_max[1] = 0u; }
+    if (tid == 0) { s_max[0] = 0u; s_max[1] = 0u; s_max[2] = 0u; }
     __syncthreads();
 
-    int cur = 0;
     for (int st = 0; st < K; st++) {
         const int dl = 1 << st;
         int64_t rlo, rhi;
@@ -302,114 +278,148 @@ __device__ __forceinline__ void mp_pass_item(const MpPassArgs& p, int64_t j, int
             const int64_t rem = (int64_t(1) << p.K) - (int64_t(2) << st);   // block halo = 2^K - 1
             rlo = max(wlo - rem, (int64_t)0); rhi = min(whi + rem, nr);
         }
-        const float4* S = fsm + cur * 3 * TRm;
-        float4* N = fsm + (cur ^ 1) * 3 * TRm;
+        // Rows [klo, khi) (local k = t - t0) are computed.  A row without a
+        // neighbour at distance dl has exactly zero coupling towards it (the
+        // boundary blocks are zero at level 0 and stay zero), so the
+        // neighbour index is clamped into the tile instead of branching: the
+        // clamped row is finite and enters multiplied by zero.
+        const int klo = (int)(rlo - t0), khi = (int)(rhi - t0);
         float lmax = 0.0f;
+#pragma unroll
         for (int q = 0; q < RPT; q++) {
             const int k = tid + q * bd;
-            const int64_t t = t0 + k;
-            if (k < TR && t >= rlo && t < rhi) {
-                const M2 Lk = m2(S[3 * k]), Uk = m2(S[3 * k + 1]);
-                const float4 yk = S[3 * k + 2];
-                float y0 = yk.x, y1 = yk.y;
-                M2 Dn = {1.0f, 0.0f, 0.0f, 1.0f}, Ln = {0, 0, 0, 0}, Un = {0, 0, 0, 0};
-                if (t - dl >= 0) {
-                    const int km = 3 * (k - dl);
-                    const M2 Lm = m2(S[km]), Um = m2(S[km + 1]);
-                    const float4 ym = S[km + 2];
-                    const M2 LU = mmul(Lk, Um), LL = mmul(Lk, Lm);
-                    Dn = {Dn.m0 - LU.m0, Dn.m1 - LU.m1, Dn.m2 - LU.m2, Dn.m3 - LU.m3};
-                    Ln = {-LL.m0, -LL.m1, -LL.m2, -LL.m3};
-                    y0 = fmaf(-Lk.m0, ym.x, fmaf(-Lk.m1, ym.y, y0));
-                    y1 = fmaf(-Lk.m2, ym.x, fmaf(-Lk.m3, ym.y, y1));
-                }
-                if (t + dl <= nr - 1) {
-                    const int kp = 3 * (k + dl);
-                    const M2 Lp = m2(S[kp]), Up = m2(S[kp + 1]);
-                    const float4 yp = S[kp + 2];
-                    const M2 UL = mmul(Uk, Lp), UU = mmul(Uk, Up);
-                    Dn = {Dn.m0 - UL.m0, Dn.m1 - UL.m1, Dn.m2 - UL.m2, Dn.m3 - UL.m3};
-                    Un = {-UU.m0, -UU.m1, -UU.m2, -UU.m3};
-                    y0 = fmaf(-Uk.m0, yp.x, fmaf(-Uk.m1, yp.y, y0));
-                    y1 = fmaf(-Uk.m2, yp.x, fmaf(-Uk.m3, yp.y, y1));
-                }
+            if (k >= klo && k < khi) {
+                const M2 Lk = Lr[q], Uk = Ur[q];
+                const int km = max(k - dl, 0), kp = min(k + dl, TR - 1);
+                const M2 Lm = m2(sL[km]), Um = m2(sU[km]), Lp = m2(sL[kp]), Up = m2(sU[kp]);
+                const float2 ym = sY[km], yp = sY[kp];
+                // D' = I - L_k U_{k-d} - U_k L_{k+d}
+                M2 Dn;
+                Dn.m0 = fmaf(-Uk.m1, Lp.m2, fmaf(-Uk.m0, Lp.m0, fmaf(-Lk.m1, Um.m2, fmaf(-Lk.m0, Um.m0, 1.0f))));
+                Dn.m1 = fmaf(-Uk.m1, Lp.m3, fmaf(-Uk.m0, Lp.m1, fmaf(-Lk.m1, Um.m3, -Lk.m0 * Um.m1)));
+                Dn.m2 = fmaf(-Uk.m3, Lp.m2, fmaf(-Uk.m2, Lp.m0, fmaf(-Lk.m3, Um.m2, -Lk.m2 * Um.m0)));
+                Dn.m3 = fmaf(-Uk.m3, Lp.m3, fmaf(-Uk.m2, Lp.m1, fmaf(-Lk.m3, Um.m3, fmaf(-Lk.m2, Um.m1, 1.0f))));
+                // Y' = Y_k - L_k Y_{k-d} - U_k Y_{k+d}
+                const float y0 = fmaf(-Uk.m1, yp.y, fmaf(-Uk.m0, yp.x, fmaf(-Lk.m1, ym.y, fmaf(-Lk.m0, ym.x, Yr[q].x))));
+                const float y1 = fmaf(-Uk.m3, yp.y, fmaf(-Uk.m2, yp.x, fmaf(-Lk.m3, ym.y, fmaf(-Lk.m2, ym.x, Yr[q].y))));
+                const M2 LL = mmul(Lk, Lm), UU = mmul(Uk, Up);
+                // L' = -D'^-1 L_k L_{k-d},  U' = -D'^-1 U_k U_{k+d},  Y' <- D'^-1 Y'
                 const M2 Mi = minv(Dn);
-                const float4 L2 = f4(mmul(Mi, Ln)), U2 = f4(mmul(Mi, Un));
-                N[3 * k] = L2;
-                N[3 * k + 1] = U2;
-                N[3 * k + 2] = make_float4(fmaf(Mi.m0, y0, Mi.m1 * y1), fmaf(Mi.m2, y0, Mi.m3 * y1), 0.0f, 0.0f);
-                if (p.final_step) lmax = fmaxf(lmax, fmaxf(amax4(L2), amax4(U2)));
+                const M2 Mn = {-Mi.m0, -Mi.m1, -Mi.m2, -Mi.m3};
+                Lr[q] = mmul(Mn, LL);
+                Ur[q] = mmul(Mn, UU);
+                Yr[q] = make_float2(fmaf(Mi.m0, y0, Mi.m1 * y1), fmaf(Mi.m2, y0, Mi.m3 * y1));
+                if (p.final_step) lmax = fmaxf(lmax, fmaxf(amaxm(Lr[q]), amaxm(Ur[q])));
             }
         }
-        cur ^= 1;
         if (p.final_step) {
-            // truncation test over the whole subsystem (one barrier per stride)
             lmax = warp_max(lmax);
             if ((tid & 31) == 0) atomicMax(&s_max[st & 1], __float_as_uint(lmax));
-            __syncthreads();
+        }
+        __syncthreads();                                   // every read of this stride is done
+        bool stop = st == K - 1;
+        if (p.final_step) {
+            // truncation test over the whole subsystem
             const float smax = __uint_as_float(s_max[st & 1]);
             if (tid == 0) s_max[(st + 1) & 1] = 0u;
-            if (!(smax >= kTrunc)) break;                    // (nan also stops: the refinement will report it)
-            __syncthreads();
-        } else {
-            __syncthreads();
+            if (!(smax >= kTrunc)) stop = true;            // (nan also stops: the refinement will report it)
         }
+        if (stop) break;
+#pragma unroll
+        for (int q = 0; q < RPT; q++) {
+            const int k = tid + q * bd;
+            if (k >= klo && k < khi) { sL[k] = f4(Lr[q]); sU[k] = f4(Ur[q]); sY[k] = Yr[q]; }
+        }
+        __syncthreads();
     }
 
-    const float4* S = fsm + cur * 3 * TRm;
     if (p.final_step) {
         // X = Y: write the correction rows and the system's |dx| maximum
         float lmax = 0.0f;
+#pragma unroll
         for (int q = 0; q < RPT; q++) {
             const int k = tid + q * bd;
             if (k < TR) {
-                const int64_t kb = r + k * p.G;                 // block row within the system
-                const int64_t i0 = 2 * kb;
-                const float4 xv = S[3 * k + 2];
-                p.dx[j * p.n + i0] = xv.x;
-                lmax = fmaxf(lmax, fabsf(xv.x));
-                if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = xv.y; lmax = fmaxf(lmax, fabsf(xv.y)); }
+                const int64_t i0 = 2 * (r + k * p.G);       // first row of the block row
+                p.dx[j * p.n + i0] = Yr[q].x;
+                lmax = fmaxf(lmax, fabsf(Yr[q].x));
+                if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = Yr[q].y; lmax = fmaxf(lmax, fabsf(Yr[q].y)); }
             }
         }
         lmax = warp_max(lmax);
         if ((tid & 31) == 0) atomic_max_pos(&p.ndx[(int64_t)p.sweep * p.m + j], lmax);
     } else {
         float lmax = 0.0f;
+#pragma unroll
         for (int q = 0; q < RPT; q++) {
             const int k = tid + q * bd;
             const int64_t t = t0 + k;
             if (k < TR && t >= wlo && t < whi) {
                 const int64_t gi = g0 + t * p.G;
-                const float4 Lv = S[3 * k], Uv = S[3 * k + 1], yv = S[3 * k + 2];
-                p.dstLU[2 * gi] = Lv;
-                p.dstLU[2 * gi + 1] = Uv;
-                p.dstY[gi] = make_float2(yv.x, yv.y);
-                lmax = fmaxf(lmax, fmaxf(amax4(Lv), amax4(Uv)));
+                p.dstLU[2 * gi] = f4(Lr[q]);
+                p.dstLU[2 * gi + 1] = f4(Ur[q]);
+                p.dstY[gi] = Yr[q];
+                lmax = fmaxf(lmax, fmaxf(amaxm(Lr[q]), amaxm(Ur[q])));
             }
         }
         lmax = warp_max(lmax);
-        if ((tid & 31) == 0 && p.trunc_out) atomic_max_pos(&p.trunc_out[j], lmax);
+        if ((tid & 31) == 0) {
+            atomic_max_pos(&p.trunc_out[j], lmax);
+            atomic_max_pos(&s_max[2], lmax);
+        }
+        __syncthreads();
+        // A window whose couplings all vanished is decoupled: its rows already
+        // hold X = Y.  Write them now; if every window of the system is
+        // decoupled the later passes of this sweep skip the system.
+        if (__uint_as_float(s_max[2]) < kTrunc) {
+            float xm = 0.0f;
+#pragma unroll
+            for (int q = 0; q < RPT; q++) {
+                const int k = tid + q * bd;
+                const int64_t t = t0 + k;
+                if (k < TR && t >= wlo && t < whi) {
+                    const int64_t i0 = 2 * (r + t * p.G);
+                    p.dx[j * p.n + i0] = Yr[q].x;
+                    xm = fmaxf(xm, fabsf(Yr[q].x));
+                    if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = Yr[q].y; xm = fmaxf(xm, fabsf(Yr[q].y)); }
+                }
+            }
+            xm = warp_max(xm);
+            if ((tid & 31) == 0) atomic_max_pos(&p.ndx_pre_out[j], xm);
+        }
     }
 }
 
+// 4 CTAs per SM up to 4 rows per thread (64 registers, 40 KB of shared
+// memory each at 1024 block rows), 2 beyond
 template <int RPT>
-__global__ void __launch_bounds__(kMpThreads)
+__global__ void __launch_bounds__(kMpThreads, RPT >= 8 ? 2 : 4)
 mp_pass_kernel(MpPassArgs p)
 {
     extern __shared__ float4 fsm[];
-    __shared__ unsigned s_max[2];
-    // grid-stride over the items, so that a pass whose systems are all
-    // finished costs a few hundred CTAs, not one CTA per item
+    __shared__ unsigned s_max[3];
+    // the flags read here were written by earlier kernels: read-only cache
+    if (__ldg(p.live) == 0) return;               // every system finished in an earlier sweep
+    float4* sL = fsm;
+    float4* sU = fsm + p.TRmax;
+    float2* sY = reinterpret_cast<float2*>(fsm + 2 * p.TRmax);
+    // grid-stride over the items (about one wave of CTAs)
     const int64_t items = p.m * p.G * p.nwin;
     for (int64_t blk = blockIdx.x; blk < items; blk += gridDim.x) {
         const int64_t item = blk / p.nwin;
         const int64_t w = blk - item * p.nwin;
         const int64_t j = item / p.G;
         const int64_t r = item - j * p.G;
-        if (p.fin[j]) continue;
-        // a system whose couplings vanished in an earlier pass is already decoupled
-        if (p.trunc_in && __uint_as_float(p.trunc_in[j]) < kTrunc) mp_copy_item(p, j, r, w);
-        else mp_pass_item<RPT>(p, j, r, w, fsm, s_max);
+        if (__ldg(p.fin + j)) continue;
+        if (p.trunc_in && __uint_as_float(__ldg(p.trunc_in + j)) < kTrunc) {
+            // Every window of the previous pass found itself decoupled and
+            // wrote its rows of dx (X = Y): item (0, 0) carries the |dx|
+            // maximum they left into the sweep's norm, the rest is skipped.
+            if (r == 0 && w == 0 && threadIdx.x == 0)
+                atomicMax(&p.ndx[(int64_t)p.sweep * p.m + j], p.ndx_pre_in[j]);
+            continue;
+        }
+        mp_pass_item<RPT>(p, j, r, w, sL, sU, sY, s_max);
         __syncthreads();
     }
 }
@@ -422,12 +432,36 @@ __device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64
     const int s = p.sweep;
     const int tid = threadIdx.x;
     const int64_t n = p.n;
+    constexpr int XR = kMpTile / kMpThreads;             // rows per thread
+
+    // Rows t0 + tid + u*kMpThreads of the tile [t0, t1); threads 0-3 also take
+    // the halo rows t0-2, t0-1, t1, t1+1 of x, recomputed bit-identically by
+    // the neighbouring tiles.  The x loads go first, then the norms the
+    // decision needs, then the bands: one memory round trip in sweep 0 (no
+    // decision to wait for) and in a last sweep (no bands to read).
+    const int64_t t0 = tile * kMpTile;
+    const int64_t t1 = min(t0 + kMpTile, n);
+    const int64_t ih = tid < 2 ? t0 - 2 + tid : t1 + tid - 2;          // halo row of threads 0-3
+    const bool halo = tid < 4 && ih >= 0 && ih < n;
+    // x_{s-1} comes from the other ping-pong buffer: neighbouring tiles read
+    // their halo rows from it while this tile writes x_s
+    const double* __restrict__ xprev = p.X[(s + 1) & 1] + j * n;
+    const float* __restrict__ dxs = p.dx + j * n;
+    float dv[XR], dvh = 0.0f;
+    double xv[XR], xvh = 0.0;
+#pragma unroll
+    for (int u = 0; u < XR; u++) {
+        const int64_t i = t0 + tid + u * kMpThreads;
+        dv[u] = 0.0f; xv[u] = 0.0;
+        if (i < t1) { dv[u] = dxs[i]; if (s > 0) xv[u] = xprev[i]; }
+    }
+    if (halo) { dvh = dxs[ih]; if (s > 0) xvh = xprev[ih]; }
 
     // per-system decision from the norms the previous kernels left behind
-    const float nd = __uint_as_float(p.ndx[(int64_t)s * p.m + j]);
     bool done = false;
     float est = 0.0f;
     if (s >= 1) {
+        const float nd = __uint_as_float(p.ndx[(int64_t)s * p.m + j]);
         const float ndp = __uint_as_float(p.ndx[(int64_t)(s - 1) * p.m + j]);
         const float nxp = __uint_as_float(p.nx[(int64_t)(s - 1) * p.m + j]);
         if (nd == 0.0f) { done = true; est = 0.0f; }
@@ -449,28 +483,33 @@ __device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64
     const bool last = done || s == p.max_sweeps - 1;
     const bool to_user = last && !p.keep_x;
 
-    // x_new on rows [t0-2, t0+TILE+2) (the halo rows are recomputed bit-identically by neighbours)
-    const int64_t t0 = tile * kMpTile;
-    const int64_t t1 = min(t0 + kMpTile, n);
-    const int64_t h0 = max(t0 - 2, (int64_t)0), h1 = min(t1 + 2, n);
-    // x_{s-1} comes from the other ping-pong buffer: neighbouring tiles read
-    // their halo rows from it while this tile writes x_s
-    const double* __restrict__ xprev = p.X[(s + 1) & 1];
-    for (int64_t i = h0 + tid; i < h1; i += blockDim.x) {
-        const double dxi = f2d(p.dx[j * n + i]);
-        sx[i - t0 + 2] = s == 0 ? dxi : __dadd_rn(xprev[j * n + i], dxi);
-    }
-    __syncthreads();
-
+    // bands and y of this thread's rows, for the residual (not read in a last sweep)
     const int64_t ybase = j * p.ss;
-    float xmax = 0.0f;
-    for (int64_t i = t0 + tid; i < t1; i += blockDim.x) {
-        const double xi = sx[i - t0 + 2];
-        if (to_user) p.y[ybase + i * p.rs] = xi;
-        else if (last) p.Xout[j * n + i] = xi;
-        else p.X[s & 1][j * n + i] = xi;
-        xmax = fmaxf(xmax, fabsf(d2f_scaled(xi, 0)));     // |x| in FP32: it only feeds the estimate
+    double ba[XR], bb[XR], bc[XR], bd[XR], be[XR], by[XR];
+#pragma unroll
+    for (int u = 0; u < XR; u++) {
+        const int64_t i = t0 + tid + u * kMpThreads;
+        ba[u] = 0.0; bb[u] = 0.0; bc[u] = 1.0; bd[u] = 0.0; be[u] = 0.0; by[u] = 0.0;
+        if (!last && i < t1) {
+            const int64_t g = ybase + i * p.rs;
+            ba[u] = p.a[g]; bb[u] = p.b[g]; bc[u] = p.c[g]; bd[u] = p.d[g]; be[u] = p.e[g]; by[u] = p.y[g];
+        }
     }
+
+    float xmax = 0.0f;
+#pragma unroll
+    for (int u = 0; u < XR; u++) {
+        const int64_t i = t0 + tid + u * kMpThreads;
+        if (i < t1) {
+            const double xi = s == 0 ? f2d(dv[u]) : __dadd_rn(xv[u], f2d(dv[u]));
+            sx[tid + u * kMpThreads + 2] = xi;
+            if (to_user) p.y[ybase + i * p.rs] = xi;
+            else if (last) p.Xout[j * n + i] = xi;
+            else p.X[s & 1][j * n + i] = xi;
+            xmax = fmaxf(xmax, fabsf(d2f_scaled(xi, 0)));     // |x| in FP32: it only feeds the estimate
+        }
+    }
+    if (halo) sx[ih - t0 + 2] = s == 0 ? f2d(dvh) : __dadd_rn(xvh, f2d(dvh));
     xmax = warp_max(xmax);
     if ((tid & 31) == 0) s_red[tid >> 5] = xmax;
     __syncthreads();
@@ -482,43 +521,54 @@ __device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64
             p.est[j] = est;
             p.status[j] = done ? 1 : 2;      // 2: stopped at max_sweeps
             p.fin[j] = s + 1;
+            for (int s2 = s + 1; s2 <= p.max_sweeps; s2++) atomicSub(&p.live[s2], 1);
         }
     }
     if (last) return;
 
-    // residual r = y - A x (FP64, FMA chain), row-scaled to FP32 and normalised
-    // by the block's diagonal inverse -> right-hand side of the next FP32 solve
+    // residual r = y - A x (FP64, FMA chain), row-scaled to FP32; the two rows
+    // of a block row sit in lanes 2k, 2k+1 and meet by a shuffle, and the even
+    // lane normalises by the block's diagonal inverse -> the next FP32 rhs
     const int64_t nb = (n + 1) / 2;
-    const int64_t T = p.m * nb;
-    for (int64_t kb = t0 / 2 + tid; 2 * kb < t1; kb += blockDim.x) {
-        const PairRow P = load_pair(p, ybase, 2 * kb);
-        const BlockRow B = block_of(P, 2 * kb, n);
-        float rf[2] = {0.0f, 0.0f};
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int64_t i = 2 * kb + h;
-            if (i < n) {
-                const int li = (int)(i - t0 + 2);
-                double r = h ? P.y1 : P.y0;
-                r = fma(-(h ? P.c1 : P.c0), sx[li], r);
-                if (i >= 2) r = fma(-(h ? P.a1 : P.a0), sx[li - 2], r);
-                if (i >= 1) r = fma(-(h ? P.b1 : P.b0), sx[li - 1], r);
-                if (i + 1 < n) r = fma(-(h ? P.d1 : P.d0), sx[li + 1], r);
-                if (i + 2 < n) r = fma(-(h ? P.e1 : P.e0), sx[li + 2], r);
-                rf[h] = d2f_scaled(r, h == 0 ? B.sh0 : B.sh1);
-            }
+    for (int u = 0; u < XR; u++) {
+        const int64_t i = t0 + tid + u * kMpThreads;
+        float rf = 0.0f, cs = 1.0f, os = 0.0f;             // r, c and the off-diagonal entry of D, scaled
+        if (i < t1) {
+            const int li = tid + u * kMpThreads + 2;
+            double r = by[u];
+            r = fma(-bc[u], sx[li], r);
+            if (i >= 2) r = fma(-ba[u], sx[li - 2], r);
+            if (i >= 1) r = fma(-bb[u], sx[li - 1], r);
+            if (i + 1 < n) r = fma(-bd[u], sx[li + 1], r);
+            if (i + 2 < n) r = fma(-be[u], sx[li + 2], r);
+            const int sh = d_exponent(bc[u]);
+            rf = d2f_scaled(r, sh);
+            cs = d2f_scaled(bc[u], sh);
+            // D = {c0, d0; b1, c1}: the even row contributes d, the odd row b
+            if ((i & 1) == 0) os = i + 1 < n ? d2f_scaled(bd[u], sh) : 0.0f;
+            else os = d2f_scaled(bb[u], sh);
         }
-        const M2 Mi = minv(B.D);
-        const int64_t q = j * nb + kb;
-        p.R[q] = make_float2(fmaf(Mi.m0, rf[0], Mi.m1 * rf[1]), fmaf(Mi.m2, rf[0], Mi.m3 * rf[1]));
+        const float rf1 = __shfl_xor_sync(0xffffffffu, rf, 1);
+        const float cs1 = __shfl_xor_sync(0xffffffffu, cs, 1);
+        const float os1 = __shfl_xor_sync(0xffffffffu, os, 1);
+        if (i < t1 && (i & 1) == 0) {
+            // the odd partner of row n-1 (odd n) is the identity row: c 1, b 0, r 0
+            const bool dummy = i + 1 >= n;
+            const M2 Mi = minv({cs, os, dummy ? 0.0f : os1, dummy ? 1.0f : cs1});
+            const float r1 = dummy ? 0.0f : rf1;
+            p.R[j * nb + (i >> 1)] = make_float2(fmaf(Mi.m0, rf, Mi.m1 * r1), fmaf(Mi.m2, rf, Mi.m3 * r1));
+        }
     }
 }
 
-__global__ void __launch_bounds__(kMpThreads)
+// 3 CTAs per SM (at most 85 registers): 3072 rows in flight per SM
+__global__ void __launch_bounds__(kMpThreads, 3)
 mp_update_kernel(MpArgs p)
 {
     __shared__ double sx[kMpTile + 4];
     __shared__ float s_red[kMpThreads / 32];
+    if (__ldg(p.live + p.sweep) == 0) return;      // every system finished in an earlier sweep
     const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
     for (int64_t blk = blockIdx.x; blk < p.m * tiles; blk += gridDim.x) {
         const int64_t j = blk / tiles;
@@ -598,12 +648,15 @@ resid_norm_kernel(const double* __restrict__ a, const double* __restrict__ b, co
     }
 }
 
+// shared memory of the pass kernel: L, U (float4) and Y (float2) per block row
+size_t mp_pass_smem(int rows) { return (size_t)rows * (2 * sizeof(float4) + sizeof(float2)); }
+
 template <int RPT>
 cudaError_t launch_mp_pass_rpt(const MpPassArgs& p, int threads, int64_t blocks, cudaStream_t s)
 {
-    const size_t smem = (size_t)6 * p.TRmax * sizeof(float4);
+    const size_t smem = mp_pass_smem(p.TRmax);
     cudaError_t e = cudaFuncSetAttribute(mp_pass_kernel<RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(6 * kMpMaxRows * sizeof(float4)));
+                                         (int)mp_pass_smem(kMpMaxRows));
     if (e != cudaSuccess) return e;
     blocks = std::min<int64_t>(blocks, mp_grid_cap((const void*)mp_pass_kernel<RPT>, threads, smem));
     mp_pass_kernel<RPT><<<(unsigned)blocks, threads, smem, s>>>(p);
@@ -640,8 +693,11 @@ cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s)
 
 cudaError_t launch_mp_update(const MpArgs& p, cudaStream_t s)
 {
+    // one CTA per tile: the tiles of a sweep are latency-bound FP64 and HBM
+    // work that needs every resident CTA; a sweep with nothing left returns
+    // at once through the live count
     const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
-    const int64_t blocks = std::min<int64_t>(p.m * tiles, mp_grid_cap((const void*)mp_update_kernel, kMpThreads, 0));
+    const int64_t blocks = std::min<int64_t>(p.m * tiles, 0x7fffffffLL);
     mp_update_kernel<<<(unsigned)blocks, kMpThreads, 0, s>>>(p);
     count_launch();
     return cudaGetLastError();

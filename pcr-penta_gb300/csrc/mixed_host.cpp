@@ -42,7 +42,7 @@ MpPlan mp_plan(int64_t nb, const pcrp_opts* o)
 }
 
 struct MpLayout {
-    size_t S0, R, P0, P1, dx, X0, X1, Xout, ndx, nx, fin, status, est, trunc, rbuf, rn, total;
+    size_t S0, R, P0, P1, dx, X0, X1, Xout, ndx, nx, fin, status, est, trunc, ndx_pre, live, rbuf, rn, total;
 };
 
 MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool info)
@@ -65,6 +65,8 @@ MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool 
     L.status = take(m * sizeof(int));
     L.est = take(m * sizeof(float));
     L.trunc = take((size_t)kMpMaxPasses * m * sizeof(unsigned));
+    L.ndx_pre = take((size_t)max_sweeps * kMpMaxPasses * m * sizeof(unsigned));
+    L.live = take((size_t)(max_sweeps + 1) * sizeof(int));
     L.rbuf = info ? take((size_t)m * n * sizeof(double)) : 0;
     L.rn = info ? take(3 * m * sizeof(unsigned)) : 0;
     L.total = off;
@@ -112,6 +114,8 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     A.fin = reinterpret_cast<int*>(base + WL.fin);
     A.status = reinterpret_cast<int*>(base + WL.status);
     A.est = F(WL.est); A.trunc = U(WL.trunc);
+    A.ndx_pre = U(WL.ndx_pre);
+    A.live = reinterpret_cast<int*>(base + WL.live);
     A.max_sweeps = max_sweeps; A.tol = (float)tol; A.keep_x = keep_x;
     {
         const void* ptrs[6] = {a, b, c, d, e, y};
@@ -127,8 +131,9 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
         // FP32 block-PCR solve of the normalised system with rhs R
         MpPassArgs p{};
         p.srcLU = A.S0; p.srcY = A.R;
-        p.dx = A.dx; p.fin = A.fin; p.ndx = A.ndx;
+        p.dx = A.dx; p.fin = A.fin; p.ndx = A.ndx; p.live = A.live + s;
         p.m = m; p.n = n; p.nb = nb; p.G = 1; p.sweep = s;
+        unsigned* pre = A.ndx_pre + (size_t)s * kMpMaxPasses * m;
         int done = 0, pass = 0;
         while (done < pl.s1) {
             const int K = std::min(pl.fuse, pl.s1 - done);
@@ -143,6 +148,8 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
             p.TRmax = (int)std::min<int64_t>(Lw + 2 * H, nrmax);
             p.trunc_in = pass > 0 ? A.trunc + (pass - 1) * m : nullptr;
             p.trunc_out = A.trunc + pass * m;
+            p.ndx_pre_in = pass > 0 ? pre + (pass - 1) * m : nullptr;
+            p.ndx_pre_out = pre + pass * m;
             ce = launch_mp_pass(p, st);
             if (ce != cudaSuccess) return cuda_error(ce, "mixed global pass launch");
             p.srcLU = p.dstLU; p.srcY = p.dstY;
@@ -154,6 +161,8 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
         p.K = Kf; p.H = 0; p.L = (int)nrmax; p.final_step = 1; p.nwin = 1; p.TRmax = (int)nrmax;
         p.trunc_in = pass > 0 ? A.trunc + (pass - 1) * m : nullptr;
         p.trunc_out = nullptr;
+        p.ndx_pre_in = pass > 0 ? pre + (pass - 1) * m : nullptr;
+        p.ndx_pre_out = nullptr;
         ce = launch_mp_pass(p, st);
         if (ce != cudaSuccess) return cuda_error(ce, "mixed shared-memory pass launch");
         // FP64 update, stopping decision, next residual

@@ -5,8 +5,8 @@
 
 namespace pcrp {
 
-constexpr int kMpTile = 1024;      // rows per CTA of the refinement kernel (even)
-constexpr int kMpMaxRows = 2048;   // block rows per CTA of the FP32 PCR kernel (2 x 48 bytes each)
+constexpr int kMpTile = 1024;      // rows per CTA of the refinement kernel (4 per thread)
+constexpr int kMpMaxRows = 2048;   // block rows per CTA of the FP32 PCR kernel (40 bytes each)
 constexpr int kMpMaxPasses = 24;   // global FP32 passes per solve
 
 // Whole-batch arguments (prep and refinement kernels).
@@ -25,6 +25,8 @@ struct MpArgs {
     int* status;                        // per system: 1 converged, 2 stopped at max_sweeps
     float* est;                         // per system: estimated relative forward error
     unsigned* trunc;                    // [kMpMaxPasses x m] max |L|,|U| after each global pass
+    unsigned* ndx_pre;                  // [max_sweeps x kMpMaxPasses x m] max |dx| written early by a global pass
+    int* live;                          // [max_sweeps + 1] systems still running at the start of each sweep
     int sweep, max_sweeps, keep_x;
     int vec;                            // 1: all six caller arrays are 16-byte aligned (paired loads allowed)
     float tol;
@@ -41,6 +43,9 @@ struct MpPassArgs {
     unsigned* ndx;                      // final pass: max |dx| of this sweep
     const unsigned* trunc_in;           // previous pass's max |L|,|U| (or null)
     unsigned* trunc_out;                // this pass's max |L|,|U| (non-final)
+    const unsigned* ndx_pre_in;         // max |dx| the previous pass wrote for decoupled windows (or null)
+    unsigned* ndx_pre_out;              // same, written by this pass (non-final)
+    const int* live;                    // systems still running in this sweep (0: the kernel returns at once)
     int64_t m, n, nb, G, nwin;
     int K, final_step, L, H, TRmax, sweep;
 };
