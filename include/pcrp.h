@@ -71,6 +71,9 @@ typedef struct pcrp_opts {
                                   unsatisfiable (bounded, ~4 ms) to test PCRP_ETIMEOUT       */
     void*    workspace;        /* caller-provided device scratch, or NULL                    */
     size_t   workspace_bytes;
+    int32_t  window_levels;    /* pcrp_solve_mixed, systems larger than one shared-memory
+                                  tile: cyclic-reduction levels of the windowed first pass
+                                  (0: 5; negative: no windowed pass, block-PCR passes only) */
 } pcrp_opts;
 
 /* Per-call report of the mixed-precision solver (host memory). */

@@ -43,7 +43,12 @@ namespace {
 
 constexpr float kTrunc = 1e-10f;
 constexpr int kMpThreads = 256;
+constexpr int kMpTryThreads = 256;
 static_assert(kMpTile % kMpThreads == 0 && kMpThreads % 2 == 0, "refinement tiles: whole rows per thread, pairs in adjacent lanes");
+// rows allocated per shared-memory array of the pass kernel (whole groups of
+// 8, the span of the swizzle of the whole-subsystem pass)
+__host__ __device__ __forceinline__ int mp_pass_rows(int rows) { return (rows + 7) & ~7; }
+
 // CTAs of one wave of a kernel (the pass kernel strides over its items with
 // one wave, so that sweeps of mostly finished systems stay cheap)
 int mp_grid_cap(const void* kernel, int threads, size_t smem)
@@ -218,6 +223,8 @@ mp_prep_kernel(MpArgs p)
         }
         for (int64_t q = threadIdx.x; q < (int64_t)p.max_sweeps * kMpMaxPasses * p.m; q += blockDim.x)
             p.ndx_pre[q] = 0u;
+        for (int64_t q = threadIdx.x; q < p.m; q += blockDim.x) p.fail[q] = 0;
+        if (threadIdx.x == 0) *p.nfail = 0;
         for (int q = threadIdx.x; q <= p.max_sweeps; q += blockDim.x) p.live[q] = (int)p.m;
     }
 }
@@ -231,11 +238,35 @@ __device__ __forceinline__ float amaxm(const M2& a) {
 __device__ __forceinline__ M2 m2(const float4& v) { return {v.x, v.y, v.z, v.w}; }
 __device__ __forceinline__ float4 f4(const M2& a) { return make_float4(a.m0, a.m1, a.m2, a.m3); }
 
-// One window (or whole subsystem) of one FP32 block-PCR pass.  Each thread
-// keeps the rows it owns (k = tid + q*blockDim) in registers; shared memory
-// holds one copy of the level's rows (L and U as float4 arrays, Y as float2),
-// read for the two neighbours of a row and rewritten after every stride:
-// 80 bytes read and 40 written per row and stride, conflict-free.
+// One block reduction step of a normalised row k (D = I) with its neighbours
+// m = k-d and p = k+d (PCR stride and cyclic-reduction level alike):
+//     D' = I - L_k U_m - U_k L_p,  L' = -D'^-1 L_k L_m,  U' = -D'^-1 U_k U_p,
+//     Y' = D'^-1 (Y_k - L_k Y_m - U_k Y_p).
+__device__ __forceinline__ void reduce_row(const M2& Lk, const M2& Uk, float2 Yk,
+                                           const M2& Lm, const M2& Um, float2 ym,
+                                           const M2& Lp, const M2& Up, float2 yp,
+                                           M2& Lo, M2& Uo, float2& Yo)
+{
+    M2 Dn;
+    Dn.m0 = fmaf(-Uk.m1, Lp.m2, fmaf(-Uk.m0, Lp.m0, fmaf(-Lk.m1, Um.m2, fmaf(-Lk.m0, Um.m0, 1.0f))));
+    Dn.m1 = fmaf(-Uk.m1, Lp.m3, fmaf(-Uk.m0, Lp.m1, fmaf(-Lk.m1, Um.m3, -Lk.m0 * Um.m1)));
+    Dn.m2 = fmaf(-Uk.m3, Lp.m2, fmaf(-Uk.m2, Lp.m0, fmaf(-Lk.m3, Um.m2, -Lk.m2 * Um.m0)));
+    Dn.m3 = fmaf(-Uk.m3, Lp.m3, fmaf(-Uk.m2, Lp.m1, fmaf(-Lk.m3, Um.m3, fmaf(-Lk.m2, Um.m1, 1.0f))));
+    const float y0 = fmaf(-Uk.m1, yp.y, fmaf(-Uk.m0, yp.x, fmaf(-Lk.m1, ym.y, fmaf(-Lk.m0, ym.x, Yk.x))));
+    const float y1 = fmaf(-Uk.m3, yp.y, fmaf(-Uk.m2, yp.x, fmaf(-Lk.m3, ym.y, fmaf(-Lk.m2, ym.x, Yk.y))));
+    const M2 LL = mmul(Lk, Lm), UU = mmul(Uk, Up);
+    const M2 Mi = minv(Dn);
+    const M2 Mn = {-Mi.m0, -Mi.m1, -Mi.m2, -Mi.m3};
+    Lo = mmul(Mn, LL);
+    Uo = mmul(Mn, UU);
+    Yo = make_float2(fmaf(Mi.m0, y0, Mi.m1 * y1), fmaf(Mi.m2, y0, Mi.m3 * y1));
+}
+
+// One window of a global FP32 block-PCR pass (K strides at level G, halo H).
+// Each thread keeps the rows it owns (k = tid + q*blockDim) in registers;
+// shared memory holds one copy of the level's rows (L and U as float4 arrays,
+// Y as float2), read for the two neighbours of a row and rewritten after
+// every stride: 80 bytes read and 40 written per row and stride.
 template <int RPT>
 __device__ __forceinline__ void mp_pass_item(const MpPassArgs& p, int64_t j, int64_t r, int64_t w,
                                              float4* sL, float4* sU, float2* sY, unsigned* s_max)
@@ -267,64 +298,31 @@ __device__ __forceinline__ void mp_pass_item(const MpPassArgs& p, int64_t j, int
             Lr[q] = m2(lv); Ur[q] = m2(uv); Yr[q] = yv;
         }
     }
-    if (tid == 0) { s_max[0] = 0u; s_max[1] = 0u; s_max[2] = 0u; }
+    if (tid == 0) s_max[0] = 0u;
     __syncthreads();
 
     for (int st = 0; st < K; st++) {
         const int dl = 1 << st;
-        int64_t rlo, rhi;
-        if (p.final_step) { rlo = 0; rhi = nr; }
-        else {
-            const int64_t rem = (int64_t(1) << p.K) - (int64_t(2) << st);   // block halo = 2^K - 1
-            rlo = max(wlo - rem, (int64_t)0); rhi = min(whi + rem, nr);
-        }
-        // Rows [klo, khi) (local k = t - t0) are computed.  A row without a
-        // neighbour at distance dl has exactly zero coupling towards it (the
-        // boundary blocks are zero at level 0 and stay zero), so the
-        // neighbour index is clamped into the tile instead of branching: the
-        // clamped row is finite and enters multiplied by zero.
-        const int klo = (int)(rlo - t0), khi = (int)(rhi - t0);
-        float lmax = 0.0f;
+        // rows this stride must produce: the window widened by the halo the
+        // remaining strides of the pass still consume
+        const int64_t rem = (int64_t(1) << K) - (int64_t(2) << st);   // block halo = 2^K - 1
+        const int klo = (int)(max(wlo - rem, (int64_t)0) - t0);
+        const int khi = (int)(min(whi + rem, nr) - t0);
+        // A row without a neighbour at distance dl has exactly zero coupling
+        // towards it (the boundary blocks are zero at level 0 and stay zero),
+        // so the neighbour index is clamped into the tile instead of
+        // branching: the clamped row is finite and enters multiplied by zero.
 #pragma unroll
         for (int q = 0; q < RPT; q++) {
             const int k = tid + q * bd;
             if (k >= klo && k < khi) {
-                const M2 Lk = Lr[q], Uk = Ur[q];
                 const int km = max(k - dl, 0), kp = min(k + dl, TR - 1);
-                const M2 Lm = m2(sL[km]), Um = m2(sU[km]), Lp = m2(sL[kp]), Up = m2(sU[kp]);
-                const float2 ym = sY[km], yp = sY[kp];
-                // D' = I - L_k U_{k-d} - U_k L_{k+d}
-                M2 Dn;
-                Dn.m0 = fmaf(-Uk.m1, Lp.m2, fmaf(-Uk.m0, Lp.m0, fmaf(-Lk.m1, Um.m2, fmaf(-Lk.m0, Um.m0, 1.0f))));
-                Dn.m1 = fmaf(-Uk.m1, Lp.m3, fmaf(-Uk.m0, Lp.m1, fmaf(-Lk.m1, Um.m3, -Lk.m0 * Um.m1)));
-                Dn.m2 = fmaf(-Uk.m3, Lp.m2, fmaf(-Uk.m2, Lp.m0, fmaf(-Lk.m3, Um.m2, -Lk.m2 * Um.m0)));
-                Dn.m3 = fmaf(-Uk.m3, Lp.m3, fmaf(-Uk.m2, Lp.m1, fmaf(-Lk.m3, Um.m3, fmaf(-Lk.m2, Um.m1, 1.0f))));
-                // Y' = Y_k - L_k Y_{k-d} - U_k Y_{k+d}
-                const float y0 = fmaf(-Uk.m1, yp.y, fmaf(-Uk.m0, yp.x, fmaf(-Lk.m1, ym.y, fmaf(-Lk.m0, ym.x, Yr[q].x))));
-                const float y1 = fmaf(-Uk.m3, yp.y, fmaf(-Uk.m2, yp.x, fmaf(-Lk.m3, ym.y, fmaf(-Lk.m2, ym.x, Yr[q].y))));
-                const M2 LL = mmul(Lk, Lm), UU = mmul(Uk, Up);
-                // L' = -D'^-1 L_k L_{k-d},  U' = -D'^-1 U_k U_{k+d},  Y' <- D'^-1 Y'
-                const M2 Mi = minv(Dn);
-                const M2 Mn = {-Mi.m0, -Mi.m1, -Mi.m2, -Mi.m3};
-                Lr[q] = mmul(Mn, LL);
-                Ur[q] = mmul(Mn, UU);
-                Yr[q] = make_float2(fmaf(Mi.m0, y0, Mi.m1 * y1), fmaf(Mi.m2, y0, Mi.m3 * y1));
-                if (p.final_step) lmax = fmaxf(lmax, fmaxf(amaxm(Lr[q]), amaxm(Ur[q])));
+                reduce_row(Lr[q], Ur[q], Yr[q], m2(sL[km]), m2(sU[km]), sY[km], m2(sL[kp]), m2(sU[kp]), sY[kp],
+                           Lr[q], Ur[q], Yr[q]);
             }
         }
-        if (p.final_step) {
-            lmax = warp_max(lmax);
-            if ((tid & 31) == 0) atomicMax(&s_max[st & 1], __float_as_uint(lmax));
-        }
         __syncthreads();                                   // every read of this stride is done
-        bool stop = st == K - 1;
-        if (p.final_step) {
-            // truncation test over the whole subsystem
-            const float smax = __uint_as_float(s_max[st & 1]);
-            if (tid == 0) s_max[(st + 1) & 1] = 0u;
-            if (!(smax >= kTrunc)) stop = true;            // (nan also stops: the refinement will report it)
-        }
-        if (stop) break;
+        if (st == K - 1) break;
 #pragma unroll
         for (int q = 0; q < RPT; q++) {
             const int k = tid + q * bd;
@@ -333,60 +331,225 @@ __device__ __forceinline__ void mp_pass_item(const MpPassArgs& p, int64_t j, int
         __syncthreads();
     }
 
-    if (p.final_step) {
-        // X = Y: write the correction rows and the system's |dx| maximum
-        float lmax = 0.0f;
+    float lmax = 0.0f;
 #pragma unroll
-        for (int q = 0; q < RPT; q++) {
-            const int k = tid + q * bd;
-            if (k < TR) {
-                const int64_t i0 = 2 * (r + k * p.G);       // first row of the block row
-                p.dx[j * p.n + i0] = Yr[q].x;
-                lmax = fmaxf(lmax, fabsf(Yr[q].x));
-                if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = Yr[q].y; lmax = fmaxf(lmax, fabsf(Yr[q].y)); }
-            }
+    for (int q = 0; q < RPT; q++) {
+        const int k = tid + q * bd;
+        const int64_t t = t0 + k;
+        if (k < TR && t >= wlo && t < whi) {
+            const int64_t gi = g0 + t * p.G;
+            p.dstLU[2 * gi] = f4(Lr[q]);
+            p.dstLU[2 * gi + 1] = f4(Ur[q]);
+            p.dstY[gi] = Yr[q];
+            lmax = fmaxf(lmax, fmaxf(amaxm(Lr[q]), amaxm(Ur[q])));
         }
-        lmax = warp_max(lmax);
-        if ((tid & 31) == 0) atomic_max_pos(&p.ndx[(int64_t)p.sweep * p.m + j], lmax);
-    } else {
-        float lmax = 0.0f;
+    }
+    lmax = warp_max(lmax);
+    if ((tid & 31) == 0) {
+        atomic_max_pos(&p.trunc_out[j], lmax);
+        atomic_max_pos(&s_max[0], lmax);
+    }
+    __syncthreads();
+    // A window whose couplings all vanished is decoupled: its rows already
+    // hold X = Y.  Write them now; if every window of the system is
+    // decoupled the later passes of this sweep skip the system.
+    if (__uint_as_float(s_max[0]) < kTrunc) {
+        float xm = 0.0f;
 #pragma unroll
         for (int q = 0; q < RPT; q++) {
             const int k = tid + q * bd;
             const int64_t t = t0 + k;
             if (k < TR && t >= wlo && t < whi) {
-                const int64_t gi = g0 + t * p.G;
-                p.dstLU[2 * gi] = f4(Lr[q]);
-                p.dstLU[2 * gi + 1] = f4(Ur[q]);
-                p.dstY[gi] = Yr[q];
-                lmax = fmaxf(lmax, fmaxf(amaxm(Lr[q]), amaxm(Ur[q])));
+                const int64_t i0 = 2 * (r + t * p.G);
+                p.dx[j * p.n + i0] = Yr[q].x;
+                xm = fmaxf(xm, fabsf(Yr[q].x));
+                if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = Yr[q].y; xm = fmaxf(xm, fabsf(Yr[q].y)); }
             }
         }
-        lmax = warp_max(lmax);
-        if ((tid & 31) == 0) {
-            atomic_max_pos(&p.trunc_out[j], lmax);
-            atomic_max_pos(&s_max[2], lmax);
+        xm = warp_max(xm);
+        if ((tid & 31) == 0) atomic_max_pos(&p.ndx_pre_out[j], xm);
+    }
+}
+
+// Shared-memory position of row k of a cyclic-reduction tile: an XOR swizzle
+// inside each aligned group of 8 rows, so that the power-of-two strides of
+// cyclic reduction hit distinct banks (16-byte slots) for 8 consecutive
+// lanes.  The arrays are allocated for whole groups of 8 rows (mp_pass_rows).
+__device__ __forceinline__ int swz(int k) { return k ^ (((k >> 3) ^ (k >> 6) ^ (k >> 9)) & 7); }
+
+// Forward block cyclic reduction of the TR rows held (swizzled) in shared
+// memory: level l turns the rows k = 0 mod 2^(l+1) into the reduced system
+// at stride 2^(l+1), while the other rows keep their level-l equations.
+// Survivors are rewritten in place (their neighbours at a level are rows that
+// level does not write); a neighbour beyond the tile is clamped to an edge
+// row, exact at a system boundary (the coupling towards it is exactly zero)
+// and otherwise confined to rows whose results are not used.  Stops when the
+// reduced rows that rows [clo, chi) depend on are decoupled (|L|,|U| <
+// kTrunc, truncated reduction) and returns the number of levels; returns -1
+// if they are still coupled after kmax levels.  A barrier must separate the
+// loads from the call.
+__device__ __forceinline__ int cr_reduce(float4* sL, float4* sU, float2* sY, int TR, int kmax, int clo, int chi)
+{
+    const int tid = threadIdx.x, bd = blockDim.x;
+    for (int l = 0; l < kmax && (1 << l) < TR; l++) {
+        const int d = 1 << l, d2 = 2 * d;
+        const int lo = clo - d2 + 1, hi = chi + d2 - 1;
+        bool coupled = false;
+        for (int k = tid * d2; k < TR; k += bd * d2) {
+            const int sk = swz(k), sm = swz(max(k - d, 0)), sp = swz(min(k + d, TR - 1));
+            M2 Lo, Uo;
+            float2 Yo;
+            reduce_row(m2(sL[sk]), m2(sU[sk]), sY[sk], m2(sL[sm]), m2(sU[sm]), sY[sm], m2(sL[sp]), m2(sU[sp]), sY[sp],
+                       Lo, Uo, Yo);
+            sL[sk] = f4(Lo); sU[sk] = f4(Uo); sY[sk] = Yo;
+            if (k >= lo && k < hi) coupled |= fmaxf(amaxm(Lo), amaxm(Uo)) >= kTrunc;
+        }
+        // the barrier reduces the test: (nan entries do not count; a nan
+        // solution is reported by the refinement)
+        if (!__syncthreads_or(coupled)) return l + 1;
+    }
+    return TR <= 1 ? 0 : -1;
+}
+
+// Back substitution after cr_reduce: the rows left at level `top` hold
+// x = Y; x_k = Y_k - L_k x_{k-d} - U_k x_{k+d} level by level downwards,
+// written over Y.
+__device__ __forceinline__ void cr_substitute(const float4* sL, const float4* sU, float2* sY, int TR, int top)
+{
+    const int tid = threadIdx.x, bd = blockDim.x;
+    for (int l = top - 1; l >= 0; l--) {
+        const int d = 1 << l;
+        for (int k = d + tid * 2 * d; k < TR; k += bd * 2 * d) {
+            const int sk = swz(k), sm = swz(k - d), sp = swz(min(k + d, TR - 1));
+            const M2 Lk = m2(sL[sk]), Uk = m2(sU[sk]);
+            const float2 xm = sY[sm], xp = sY[sp], yk = sY[sk];
+            sY[sk] = make_float2(fmaf(-Uk.m1, xp.y, fmaf(-Uk.m0, xp.x, fmaf(-Lk.m1, xm.y, fmaf(-Lk.m0, xm.x, yk.x)))),
+                                 fmaf(-Uk.m3, xp.y, fmaf(-Uk.m2, xp.x, fmaf(-Lk.m3, xm.y, fmaf(-Lk.m2, xm.x, yk.y)))));
         }
         __syncthreads();
-        // A window whose couplings all vanished is decoupled: its rows already
-        // hold X = Y.  Write them now; if every window of the system is
-        // decoupled the later passes of this sweep skip the system.
-        if (__uint_as_float(s_max[2]) < kTrunc) {
-            float xm = 0.0f;
-#pragma unroll
-            for (int q = 0; q < RPT; q++) {
-                const int k = tid + q * bd;
-                const int64_t t = t0 + k;
-                if (k < TR && t >= wlo && t < whi) {
-                    const int64_t i0 = 2 * (r + t * p.G);
-                    p.dx[j * p.n + i0] = Yr[q].x;
-                    xm = fmaxf(xm, fabsf(Yr[q].x));
-                    if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = Yr[q].y; xm = fmaxf(xm, fabsf(Yr[q].y)); }
-                }
-            }
-            xm = warp_max(xm);
-            if ((tid & 31) == 0) atomic_max_pos(&p.ndx_pre_out[j], xm);
-        }
+    }
+}
+
+// Loads rows [t0, t0 + TR) of subsystem r (level G) of system j into the
+// swizzled tile.
+__device__ __forceinline__ void cr_load(const MpPassArgs& p, int64_t j, int64_t r, int64_t t0, int TR,
+                                        float4* sL, float4* sU, float2* sY)
+{
+    const int64_t g0 = j * p.nb + r;
+    for (int k = threadIdx.x; k < TR; k += blockDim.x) {
+        const int64_t gi = g0 + (t0 + k) * p.G;
+        const int s = swz(k);
+        sL[s] = p.srcLU[2 * gi]; sU[s] = p.srcLU[2 * gi + 1]; sY[s] = p.srcY[gi];
+    }
+    __syncthreads();
+}
+
+// dx rows of tile rows [klo, khi) (tile row k = subsystem row t0 + k of
+// subsystem r at level G) and their |dx| maximum into *norm.
+__device__ __forceinline__ void cr_store(const MpPassArgs& p, int64_t j, int64_t r, int64_t t0, int klo, int khi,
+                                         const float2* sY, unsigned* norm)
+{
+    float xmx = 0.0f;
+    for (int k = klo + threadIdx.x; k < khi; k += blockDim.x) {
+        const int64_t i0 = 2 * (r + (t0 + k) * p.G);      // first row of the block row
+        const float2 xv = sY[swz(k)];
+        p.dx[j * p.n + i0] = xv.x;
+        xmx = fmaxf(xmx, fabsf(xv.x));
+        if (i0 + 1 < p.n) { p.dx[j * p.n + i0 + 1] = xv.y; xmx = fmaxf(xmx, fabsf(xv.y)); }
+    }
+    xmx = warp_max(xmx);
+    if ((threadIdx.x & 31) == 0) atomic_max_pos(norm, xmx);
+}
+
+// A whole subsystem (nr <= TRmax rows at level G) by block cyclic reduction
+// to the top (or until truncation) and back substitution: about 2 row
+// updates per row instead of log2(nr).
+__device__ __forceinline__ void mp_final_item(const MpPassArgs& p, int64_t j, int64_t r,
+                                              float4* sL, float4* sU, float2* sY)
+{
+    if (r >= p.nb) return;
+    const int nr = (int)((p.nb - 1 - r) / p.G + 1);
+    cr_load(p, j, r, 0, nr, sL, sU, sY);
+    const int top = cr_reduce(sL, sU, sY, nr, 31, 0, nr);   // never -1 on a whole subsystem
+    cr_substitute(sL, sU, sY, nr, top);
+    cr_store(p, j, r, 0, 0, nr, sY, &p.ndx[(int64_t)p.sweep * p.m + j]);
+}
+
+// Windowed truncated cyclic reduction at level 0 (the first pass of a large
+// system): window [wlo, wlo + L) with a halo of H = 2^(K+1) rows each side.
+// After l <= K levels the reduced rows the window depends on lie within
+// 2^l - 1 rows of it and are exact when their own dependence (2^l - 1 rows
+// further) is inside the tile; if they are decoupled, back substitution
+// gives the window's dx with no other window involved.  Otherwise the system
+// is marked for the general passes (block PCR windows + shared-memory
+// finish) and the window writes nothing.
+struct TryTile {
+    int64_t j, wlo, whi, t0;
+    int TR;
+    bool whole;                                   // the tile holds the whole system
+};
+
+__device__ __forceinline__ TryTile try_tile(const MpPassArgs& p, int64_t item)
+{
+    TryTile t;
+    t.j = item / p.nwin;
+    const int64_t w = item - t.j * p.nwin;
+    t.wlo = w * (int64_t)p.L;
+    t.whi = min(t.wlo + (int64_t)p.L, p.nb);
+    t.t0 = max(t.wlo - (int64_t)p.H, (int64_t)0);
+    const int64_t t1 = min(t.whi + (int64_t)p.H, p.nb);
+    t.TR = (int)(t1 - t.t0);
+    t.whole = t.t0 == 0 && t1 == p.nb;
+    return t;
+}
+
+// next item of this CTA with work: running system, window inside it, and
+// (after sweep 0) a system the windowed pass solves
+__device__ __forceinline__ int64_t try_next(const MpPassArgs& p, int64_t item, int64_t items)
+{
+    for (; item < items; item += gridDim.x) {
+        const int64_t j = item / p.nwin;
+        if (__ldg(p.fin + j)) continue;
+        if (p.sweep > 0 && __ldg(p.fail + j)) continue;
+        if ((item - j * p.nwin) * (int64_t)p.L >= p.nb) continue;
+        break;
+    }
+    return item;
+}
+
+__device__ __forceinline__ void try_solve(const MpPassArgs& p, const TryTile& t, float4* sL, float4* sU, float2* sY)
+{
+    cr_load(p, t.j, 0, t.t0, t.TR, sL, sU, sY);
+    // a tile holding the whole system needs no truncation: reduce to the top
+    const int kmax = t.whole ? 31 : p.K;
+    const int top = cr_reduce(sL, sU, sY, t.TR, kmax, (int)(t.wlo - t.t0), (int)(t.whi - t.t0));
+    if (top < 0) {
+        if (threadIdx.x == 0 && atomicOr(&p.fail[t.j], 1) == 0) atomicAdd(p.nfail, 1);
+        return;
+    }
+    cr_substitute(sL, sU, sY, t.TR, top);
+    // |dx| goes straight into the sweep's norm: if another window of the
+    // system fails, the general passes rewrite these rows with values equal
+    // to within the truncation, so the maximum stands either way
+    cr_store(p, t.j, 0, t.t0, (int)(t.wlo - t.t0), (int)(t.whi - t.t0), sY, &p.ndx[(int64_t)p.sweep * p.m + t.j]);
+}
+
+// Persistent CTAs over the windows, 4 per SM (40 KB tiles of 1024 rows):
+// the reduction levels are short dependent chains separated by barriers, so
+// several tiles per SM keep it busy.
+__global__ void __launch_bounds__(kMpTryThreads, 4)
+mp_try_kernel(MpPassArgs p)
+{
+    extern __shared__ float4 fsm[];
+    if (__ldg(p.live) == 0) return;               // every system finished in an earlier sweep
+    const int TRs = mp_pass_rows(p.TRmax);
+    float4* sL = fsm;
+    float4* sU = fsm + TRs;
+    float2* sY = reinterpret_cast<float2*>(fsm + 2 * TRs);
+    const int64_t items = p.m * p.nwin;
+    for (int64_t it = try_next(p, blockIdx.x, items); it < items; it = try_next(p, it + gridDim.x, items)) {
+        try_solve(p, try_tile(p, it), sL, sU, sY);
+        __syncthreads();
     }
 }
 
@@ -397,12 +560,14 @@ __global__ void __launch_bounds__(kMpThreads, RPT >= 8 ? 2 : 4)
 mp_pass_kernel(MpPassArgs p)
 {
     extern __shared__ float4 fsm[];
-    __shared__ unsigned s_max[3];
+    __shared__ unsigned s_max[1];
     // the flags read here were written by earlier kernels: read-only cache
     if (__ldg(p.live) == 0) return;               // every system finished in an earlier sweep
+    if (p.fail && __ldg(p.nfail) == 0) return;    // the windowed pass solved every system
+    const int TRs = mp_pass_rows(p.TRmax);
     float4* sL = fsm;
-    float4* sU = fsm + p.TRmax;
-    float2* sY = reinterpret_cast<float2*>(fsm + 2 * p.TRmax);
+    float4* sU = fsm + TRs;
+    float2* sY = reinterpret_cast<float2*>(fsm + 2 * TRs);
     // grid-stride over the items (about one wave of CTAs)
     const int64_t items = p.m * p.G * p.nwin;
     for (int64_t blk = blockIdx.x; blk < items; blk += gridDim.x) {
@@ -411,6 +576,7 @@ mp_pass_kernel(MpPassArgs p)
         const int64_t j = item / p.G;
         const int64_t r = item - j * p.G;
         if (__ldg(p.fin + j)) continue;
+        if (p.fail && !__ldg(p.fail + j)) continue;   // solved by the windowed cyclic-reduction pass
         if (p.trunc_in && __uint_as_float(__ldg(p.trunc_in + j)) < kTrunc) {
             // Every window of the previous pass found itself decoupled and
             // wrote its rows of dx (X = Y): item (0, 0) carries the |dx|
@@ -419,7 +585,8 @@ mp_pass_kernel(MpPassArgs p)
                 atomicMax(&p.ndx[(int64_t)p.sweep * p.m + j], p.ndx_pre_in[j]);
             continue;
         }
-        mp_pass_item<RPT>(p, j, r, w, sL, sU, sY, s_max);
+        if (p.final_step) mp_final_item(p, j, r, sL, sU, sY);
+        else mp_pass_item<RPT>(p, j, r, w, sL, sU, sY, s_max);
         __syncthreads();
     }
 }
@@ -649,7 +816,7 @@ resid_norm_kernel(const double* __restrict__ a, const double* __restrict__ b, co
 }
 
 // shared memory of the pass kernel: L, U (float4) and Y (float2) per block row
-size_t mp_pass_smem(int rows) { return (size_t)rows * (2 * sizeof(float4) + sizeof(float2)); }
+size_t mp_pass_smem(int rows) { return (size_t)mp_pass_rows(rows) * (2 * sizeof(float4) + sizeof(float2)); }
 
 template <int RPT>
 cudaError_t launch_mp_pass_rpt(const MpPassArgs& p, int threads, int64_t blocks, cudaStream_t s)
@@ -691,13 +858,27 @@ cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s)
     return cudaErrorInvalidValue;
 }
 
+cudaError_t launch_mp_try(const MpPassArgs& p, cudaStream_t s)
+{
+    if (p.TRmax > kMpMaxRows) return cudaErrorInvalidValue;
+    const int64_t items = p.m * p.nwin;
+    if (items <= 0) return cudaSuccess;
+    const size_t smem = mp_pass_smem(p.TRmax);
+    cudaError_t e = cudaFuncSetAttribute(mp_try_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)mp_pass_smem(kMpMaxRows));
+    if (e != cudaSuccess) return e;
+    const int64_t blocks = std::min<int64_t>(items, mp_grid_cap((const void*)mp_try_kernel, kMpTryThreads, smem));
+    mp_try_kernel<<<(unsigned)blocks, kMpTryThreads, smem, s>>>(p);
+    count_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_mp_update(const MpArgs& p, cudaStream_t s)
 {
-    // one CTA per tile: the tiles of a sweep are latency-bound FP64 and HBM
-    // work that needs every resident CTA; a sweep with nothing left returns
-    // at once through the live count
+    // one wave of CTAs striding over the tiles: a sweep with nothing left
+    // returns at once through the live count
     const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
-    const int64_t blocks = std::min<int64_t>(p.m * tiles, 0x7fffffffLL);
+    const int64_t blocks = std::min<int64_t>(p.m * tiles, mp_grid_cap((const void*)mp_update_kernel, kMpThreads, 0));
     mp_update_kernel<<<(unsigned)blocks, kMpThreads, 0, s>>>(p);
     count_launch();
     return cudaGetLastError();

@@ -21,6 +21,7 @@ struct MpPlan {
     int fuse;       // strides per global pass
     int s1;         // global strides in total
     int npass;
+    int win;        // levels of the windowed cyclic-reduction pass (0: none)
 };
 
 MpPlan mp_plan(int64_t nb, const pcrp_opts* o)
@@ -29,10 +30,14 @@ MpPlan mp_plan(int64_t nb, const pcrp_opts* o)
     const int rows = (int)(sizeof(table) / sizeof(table[0]));
     int t = 0;
     while (t + 1 < rows && 2 * nb > table[t][0]) t++;
-    MpPlan p{(int)table[t][1], (int)table[t][2], 0, 0};
+    MpPlan p{(int)table[t][1], (int)table[t][2], 0, 0, kMpTryLevels};
+    // a system that fits one shared-memory tile is reduced whole (cyclic
+    // reduction to the top, no global pass)
+    if (nb <= kMpMaxRows) p.cap = kMpMaxRows;
     if (o && o->size >= sizeof(pcrp_opts)) {
         if (o->smem_rows > 0) p.cap = std::max(1, o->smem_rows / 2);
         if (o->fuse_strides > 0) p.fuse = o->fuse_strides;
+        if (o->window_levels != 0) p.win = std::min(std::max(o->window_levels, 0), 7);   // halo 2^(K+1) < tile/2
     }
     p.cap = std::min(std::max(p.cap, 1), kMpMaxRows);
     p.fuse = std::min(std::max(p.fuse, 1), 9);
@@ -42,7 +47,8 @@ MpPlan mp_plan(int64_t nb, const pcrp_opts* o)
 }
 
 struct MpLayout {
-    size_t S0, R, P0, P1, dx, X0, X1, Xout, ndx, nx, fin, status, est, trunc, ndx_pre, live, rbuf, rn, total;
+    size_t S0, R, P0, P1, dx, X0, X1, Xout, ndx, nx, fin, status, est, trunc, ndx_pre, live, fail, nfail, rbuf, rn,
+        total;
 };
 
 MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool info)
@@ -67,6 +73,8 @@ MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool 
     L.trunc = take((size_t)kMpMaxPasses * m * sizeof(unsigned));
     L.ndx_pre = take((size_t)max_sweeps * kMpMaxPasses * m * sizeof(unsigned));
     L.live = take((size_t)(max_sweeps + 1) * sizeof(int));
+    L.fail = take(m * sizeof(int));
+    L.nfail = take(sizeof(int));
     L.rbuf = info ? take((size_t)m * n * sizeof(double)) : 0;
     L.rn = info ? take(3 * m * sizeof(unsigned)) : 0;
     L.total = off;
@@ -116,6 +124,8 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     A.est = F(WL.est); A.trunc = U(WL.trunc);
     A.ndx_pre = U(WL.ndx_pre);
     A.live = reinterpret_cast<int*>(base + WL.live);
+    A.fail = reinterpret_cast<int*>(base + WL.fail);
+    A.nfail = reinterpret_cast<int*>(base + WL.nfail);
     A.max_sweeps = max_sweeps; A.tol = (float)tol; A.keep_x = keep_x;
     {
         const void* ptrs[6] = {a, b, c, d, e, y};
@@ -134,6 +144,19 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
         p.dx = A.dx; p.fin = A.fin; p.ndx = A.ndx; p.live = A.live + s;
         p.m = m; p.n = n; p.nb = nb; p.G = 1; p.sweep = s;
         unsigned* pre = A.ndx_pre + (size_t)s * kMpMaxPasses * m;
+        if (pl.s1 > 0 && pl.win > 0) {
+            // windowed cyclic reduction: solves the systems that decouple
+            // within pl.win levels; the passes below take the others
+            MpPassArgs t = p;
+            const int H = 2 << pl.win;
+            t.K = pl.win; t.H = H; t.L = kMpTryRows - 2 * H; t.final_step = 0;
+            t.nwin = cdiv(nb, t.L);
+            t.TRmax = (int)std::min<int64_t>(t.L + 2 * H, nb);
+            t.fail = A.fail; t.nfail = A.nfail;
+            ce = launch_mp_try(t, st);
+            if (ce != cudaSuccess) return cuda_error(ce, "mixed windowed reduction launch");
+            p.fail = A.fail; p.nfail = A.nfail;
+        }
         int done = 0, pass = 0;
         while (done < pl.s1) {
             const int K = std::min(pl.fuse, pl.s1 - done);

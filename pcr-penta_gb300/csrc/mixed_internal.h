@@ -8,6 +8,8 @@ namespace pcrp {
 constexpr int kMpTile = 1024;      // rows per CTA of the refinement kernel (4 per thread)
 constexpr int kMpMaxRows = 2048;   // block rows per CTA of the FP32 PCR kernel (40 bytes each)
 constexpr int kMpMaxPasses = 24;   // global FP32 passes per solve
+constexpr int kMpTryLevels = 5;    // levels of the windowed cyclic-reduction pass (halo 2^(K+1) rows)
+constexpr int kMpTryRows = 1024;   // rows of one window tile of that pass
 
 // Whole-batch arguments (prep and refinement kernels).
 struct MpArgs {
@@ -27,6 +29,8 @@ struct MpArgs {
     unsigned* trunc;                    // [kMpMaxPasses x m] max |L|,|U| after each global pass
     unsigned* ndx_pre;                  // [max_sweeps x kMpMaxPasses x m] max |dx| written early by a global pass
     int* live;                          // [max_sweeps + 1] systems still running at the start of each sweep
+    int* fail;                          // [m] 1: the windowed cyclic-reduction pass leaves the system coupled
+    int* nfail;                         // systems with fail set
     int sweep, max_sweeps, keep_x;
     int vec;                            // 1: all six caller arrays are 16-byte aligned (paired loads allowed)
     float tol;
@@ -46,12 +50,16 @@ struct MpPassArgs {
     const unsigned* ndx_pre_in;         // max |dx| the previous pass wrote for decoupled windows (or null)
     unsigned* ndx_pre_out;              // same, written by this pass (non-final)
     const int* live;                    // systems still running in this sweep (0: the kernel returns at once)
+    int* fail;                          // per system: the windowed cyclic-reduction pass did not decouple it
+                                        // (null: no such pass; general passes then run for every system)
+    int* nfail;                         // number of systems with fail set
     int64_t m, n, nb, G, nwin;
     int K, final_step, L, H, TRmax, sweep;
 };
 
 cudaError_t launch_mp_prep(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s);
+cudaError_t launch_mp_try(const MpPassArgs& p, cudaStream_t s);
 cudaError_t launch_mp_update(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_residual(const double* a, const double* b, const double* c, const double* d, const double* e,
                             const double* y, const double* x, double* r, int64_t m, int64_t n, int64_t ss,

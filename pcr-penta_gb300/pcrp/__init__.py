@@ -47,7 +47,8 @@ class Opts(ctypes.Structure):
     _fields_ = [("size", ctypes.c_uint32), ("smem_rows", ctypes.c_int32),
                 ("fuse_strides", ctypes.c_int32), ("tile_rows", ctypes.c_int32),
                 ("threads", ctypes.c_int32), ("reserved0", ctypes.c_int32),
-                ("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t)]
+                ("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t),
+                ("window_levels", ctypes.c_int32)]
 
     def __init__(self, **kw):
         super().__init__()

@@ -48,13 +48,39 @@ def test_mixed_benchmark_generators(cuda, kind, m, n):
     assert info.converged == 1
 
 
-@pytest.mark.parametrize("opts", [dict(smem_rows=64), dict(smem_rows=64, fuse_strides=2), dict(smem_rows=8, fuse_strides=1)])
+@pytest.mark.parametrize("opts", [
+    dict(smem_rows=64), dict(smem_rows=64, window_levels=2), dict(smem_rows=64, window_levels=7),
+    dict(smem_rows=64, window_levels=-1), dict(smem_rows=64, fuse_strides=2, window_levels=-1),
+    dict(smem_rows=8, fuse_strides=1, window_levels=-1)])
 def test_mixed_forced_global_passes(cuda, opts):
+    """Systems larger than the shared-memory tile: the windowed cyclic
+    reduction (any depth; too shallow a window leaves the systems coupled and
+    hands them to the block-PCR passes) and the block-PCR passes alone."""
     m, n = 3, 3000
     arrs = dd_bands(np.random.default_rng(7), m, n)
     x, info, _ = run_mixed(arrs, m, n, opts=pcrp.Opts(**opts))
     assert O.fwd_err(x, O.ge(*arrs, m, n), m, n) <= TOL
     assert info.converged == 1
+
+
+@pytest.mark.parametrize("n", [4097, 16384, 40000])
+def test_mixed_batch_of_decoupling_and_coupled_systems(cuda, n):
+    """One batch where the windowed cyclic reduction decouples some systems
+    (dominant) and leaves others coupled (ADI: its couplings need ~10 levels
+    to vanish); the latter go through the block-PCR passes in the same sweeps."""
+    dom = pcrp.generate(pcrp.GEN_DOMINANT, 3, 2, n)
+    adi = pcrp.generate(pcrp.GEN_ADI, 4, 2, n)
+    arrs = [np.concatenate([np.asarray(u), np.asarray(v)]) for u, v in zip(dom, adi)]
+    m = 4
+    x, info, _ = run_mixed(arrs, m, n, max_sweeps=16)
+    assert info.converged == 1
+    xt = O.ge(*arrs, m, n)
+    for _ in range(2):
+        xt = xt + O.ge(*arrs[:5], O.residual(*arrs, xt, m, n), m, n)
+    # dominant systems to the solver's bar; the ADI ones (condition up to
+    # ~1e5 at these sizes) to the bar of the ill-conditioned ADI test
+    assert O.fwd_err(x[: 2 * n], xt[: 2 * n], 2, n) <= TOL
+    assert O.fwd_err(x[2 * n:], xt[2 * n:], 2, n) <= 1e-11
 
 
 def test_mixed_ill_conditioned_adi(cuda):
