@@ -211,6 +211,7 @@ mp_prep_kernel(MpArgs p)
         const float y1 = 2 * k + 1 < p.n ? d2f_scaled(P.y1, B.sh1) : 0.0f;
         p.S0[2 * q] = make_float4(L.m0, L.m1, L.m2, L.m3);
         p.S0[2 * q + 1] = make_float4(U.m0, U.m1, U.m2, U.m3);
+        p.Mi[q] = make_float4(Mi.m0, Mi.m1, Mi.m2, Mi.m3);
         p.R[q] = make_float2(fmaf(Mi.m0, y0, Mi.m1 * y1), fmaf(Mi.m2, y0, Mi.m3 * y1));
     }
     if (blockIdx.x == 0) {
@@ -663,7 +664,9 @@ __device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64
         }
     }
 
-    float xmax = 0.0f;
+    // max |x| as the largest bit pattern with the sign cleared (non-negative
+    // doubles order like their bits; a nan wins and poisons the norm)
+    unsigned long long xbits = 0ull;
 #pragma unroll
     for (int u = 0; u < XR; u++) {
         const int64_t i = t0 + tid + u * kMpThreads;
@@ -673,10 +676,11 @@ __device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64
             if (to_user) p.y[ybase + i * p.rs] = xi;
             else if (last) p.Xout[j * n + i] = xi;
             else p.X[s & 1][j * n + i] = xi;
-            xmax = fmaxf(xmax, fabsf(d2f_scaled(xi, 0)));     // |x| in FP32: it only feeds the estimate
+            xbits = max(xbits, (unsigned long long)__double_as_longlong(xi) & 0x7FFFFFFFFFFFFFFFull);
         }
     }
     if (halo) sx[ih - t0 + 2] = s == 0 ? f2d(dvh) : __dadd_rn(xvh, f2d(dvh));
+    float xmax = d2f_scaled(__longlong_as_double((long long)xbits), 0);   // in FP32: it only feeds the estimate
     xmax = warp_max(xmax);
     if ((tid & 31) == 0) s_red[tid >> 5] = xmax;
     __syncthreads();
@@ -693,44 +697,46 @@ __device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64
     }
     if (last) return;
 
-    // residual r = y - A x (FP64, FMA chain), row-scaled to FP32; the two rows
-    // of a block row sit in lanes 2k, 2k+1 and meet by a shuffle, and the even
-    // lane normalises by the block's diagonal inverse -> the next FP32 rhs
+    // residual r = y - A x (FP64, FMA chain), row-scaled to FP32 by the power
+    // of two of its main diagonal; the odd row of a block row reaches the even
+    // lane by a shuffle, which normalises the pair by the block's diagonal
+    // inverse (left by the prep kernel) -> the next FP32 rhs
     const int64_t nb = (n + 1) / 2;
+    const bool interior = t0 >= 2 && t1 + 2 <= n;          // no band slot of the tile falls outside the system
 #pragma unroll
     for (int u = 0; u < XR; u++) {
-        const int64_t i = t0 + tid + u * kMpThreads;
-        float rf = 0.0f, cs = 1.0f, os = 0.0f;             // r, c and the off-diagonal entry of D, scaled
+        const int r0 = tid + u * kMpThreads;               // row within the tile (even lanes: first row of a block row)
+        const int64_t i = t0 + r0;
+        const bool even = (r0 & 1) == 0;
+        float4 Mi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (even && i < t1) Mi = p.Mi[j * nb + (i >> 1)];
+        float rf = 0.0f;
         if (i < t1) {
-            const int li = tid + u * kMpThreads + 2;
+            const int li = r0 + 2;
             double r = by[u];
             r = fma(-bc[u], sx[li], r);
-            if (i >= 2) r = fma(-ba[u], sx[li - 2], r);
-            if (i >= 1) r = fma(-bb[u], sx[li - 1], r);
-            if (i + 1 < n) r = fma(-bd[u], sx[li + 1], r);
-            if (i + 2 < n) r = fma(-be[u], sx[li + 2], r);
-            const int sh = d_exponent(bc[u]);
-            rf = d2f_scaled(r, sh);
-            cs = d2f_scaled(bc[u], sh);
-            // D = {c0, d0; b1, c1}: the even row contributes d, the odd row b
-            if ((i & 1) == 0) os = i + 1 < n ? d2f_scaled(bd[u], sh) : 0.0f;
-            else os = d2f_scaled(bb[u], sh);
+            if (interior) {
+                r = fma(-ba[u], sx[li - 2], r);
+                r = fma(-bb[u], sx[li - 1], r);
+                r = fma(-bd[u], sx[li + 1], r);
+                r = fma(-be[u], sx[li + 2], r);
+            } else {
+                if (i >= 2) r = fma(-ba[u], sx[li - 2], r);
+                if (i >= 1) r = fma(-bb[u], sx[li - 1], r);
+                if (i + 1 < n) r = fma(-bd[u], sx[li + 1], r);
+                if (i + 2 < n) r = fma(-be[u], sx[li + 2], r);
+            }
+            rf = d2f_scaled(r, d_exponent(bc[u]));
         }
+        // (the partner of row n-1 of an odd system is the identity row of the
+        // padded block, r = 0: its lane lies past t1 and keeps rf = 0)
         const float rf1 = __shfl_xor_sync(0xffffffffu, rf, 1);
-        const float cs1 = __shfl_xor_sync(0xffffffffu, cs, 1);
-        const float os1 = __shfl_xor_sync(0xffffffffu, os, 1);
-        if (i < t1 && (i & 1) == 0) {
-            // the odd partner of row n-1 (odd n) is the identity row: c 1, b 0, r 0
-            const bool dummy = i + 1 >= n;
-            const M2 Mi = minv({cs, os, dummy ? 0.0f : os1, dummy ? 1.0f : cs1});
-            const float r1 = dummy ? 0.0f : rf1;
-            p.R[j * nb + (i >> 1)] = make_float2(fmaf(Mi.m0, rf, Mi.m1 * r1), fmaf(Mi.m2, rf, Mi.m3 * r1));
-        }
+        if (even && i < t1)
+            p.R[j * nb + (i >> 1)] = make_float2(fmaf(Mi.x, rf, Mi.y * rf1), fmaf(Mi.z, rf, Mi.w * rf1));
     }
 }
 
-// 3 CTAs per SM (at most 85 registers): 3072 rows in flight per SM
-__global__ void __launch_bounds__(kMpThreads, 3)
+__global__ void __launch_bounds__(kMpThreads, 5)
 mp_update_kernel(MpArgs p)
 {
     __shared__ double sx[kMpTile + 4];

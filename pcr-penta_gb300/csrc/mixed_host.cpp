@@ -47,7 +47,7 @@ MpPlan mp_plan(int64_t nb, const pcrp_opts* o)
 }
 
 struct MpLayout {
-    size_t S0, R, P0, P1, dx, X0, X1, Xout, ndx, nx, fin, status, est, trunc, ndx_pre, live, fail, nfail, rbuf, rn,
+    size_t S0, R, Mi, P0, P1, dx, X0, X1, Xout, ndx, nx, fin, status, est, trunc, ndx_pre, live, fail, nfail, rbuf, rn,
         total;
 };
 
@@ -59,6 +59,7 @@ MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool 
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
     L.S0 = take(2 * T * sizeof(float4));
     L.R = take(T * sizeof(float2));
+    L.Mi = take(T * sizeof(float4));
     L.P0 = pl.s1 > 0 ? take(2 * T * sizeof(float4) + T * sizeof(float2)) : 0;
     L.P1 = pl.npass > 1 ? take(2 * T * sizeof(float4) + T * sizeof(float2)) : 0;
     L.dx = take((size_t)m * n * sizeof(float));
@@ -114,6 +115,7 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     A.m = m; A.n = n; A.ss = ss; A.rs = rs;
     A.S0 = reinterpret_cast<float4*>(base + WL.S0);
     A.R = reinterpret_cast<float2*>(base + WL.R);
+    A.Mi = reinterpret_cast<float4*>(base + WL.Mi);
     A.dx = F(WL.dx);
     A.X[0] = reinterpret_cast<double*>(base + WL.X0);
     A.X[1] = reinterpret_cast<double*>(base + WL.X1);

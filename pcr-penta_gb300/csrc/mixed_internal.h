@@ -5,7 +5,7 @@
 
 namespace pcrp {
 
-constexpr int kMpTile = 1024;      // rows per CTA of the refinement kernel (4 per thread)
+constexpr int kMpTile = 512;       // rows per CTA of the refinement kernel (2 per thread)
 constexpr int kMpMaxRows = 2048;   // block rows per CTA of the FP32 PCR kernel (40 bytes each)
 constexpr int kMpMaxPasses = 24;   // global FP32 passes per solve
 constexpr int kMpTryLevels = 5;    // levels of the windowed cyclic-reduction pass (halo 2^(K+1) rows)
@@ -18,6 +18,7 @@ struct MpArgs {
     int64_t m, n, ss, rs;
     float4* S0;                         // level-0 normalised L,U: [2*q] = L, [2*q+1] = U, q < m*nb
     float2* R;                          // normalised rhs Y of block row q
+    float4* Mi;                         // inverse of the row-scaled FP32 diagonal block of block row q
     float* dx;                          // FP32 correction, m*n (contiguous)
     double* X[2];                       // FP64 iterates, m*n each (contiguous): sweep s writes X[s&1]
     double* Xout;                       // final iterate when the caller asked for a report (keep_x)
