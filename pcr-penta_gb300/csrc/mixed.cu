@@ -60,6 +60,12 @@ int mp_grid_cap(const void* kernel, int threads, size_t smem)
     return sms * per;
 }
 
+// Programmatic dependent launch (see launch_dependent): wait for the
+// predecessor kernel's completion and memory before touching memory; allow
+// the successor to be launched (it waits in turn).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // integer-pipe conversions
 // ---------------------------------------------------------------------------
@@ -197,6 +203,7 @@ __device__ __forceinline__ BlockRow block_of(const PairRow& P, int64_t i0, int64
 __global__ void __launch_bounds__(kMpThreads)
 mp_prep_kernel(MpArgs p)
 {
+    pdl_wait();
     const int64_t nb = (p.n + 1) / 2;
     const int64_t total = p.m * nb;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
@@ -228,6 +235,7 @@ mp_prep_kernel(MpArgs p)
         if (threadIdx.x == 0) *p.nfail = 0;
         for (int q = threadIdx.x; q <= p.max_sweeps; q += blockDim.x) p.live[q] = (int)p.m;
     }
+    pdl_release();                                // (multi-wave grid: release once this CTA is done)
 }
 
 // ---------------------------------------------------------------------------
@@ -542,6 +550,8 @@ __global__ void __launch_bounds__(kMpTryThreads, 4)
 mp_try_kernel(MpPassArgs p)
 {
     extern __shared__ float4 fsm[];
+    pdl_wait();
+    pdl_release();                                // one wave of persistent CTAs: the successor may queue now
     if (__ldg(p.live) == 0) return;               // every system finished in an earlier sweep
     const int TRs = mp_pass_rows(p.TRmax);
     float4* sL = fsm;
@@ -562,6 +572,8 @@ mp_pass_kernel(MpPassArgs p)
 {
     extern __shared__ float4 fsm[];
     __shared__ unsigned s_max[1];
+    pdl_wait();
+    pdl_release();                                // one wave of persistent CTAs: the successor may queue now
     // the flags read here were written by earlier kernels: read-only cache
     if (__ldg(p.live) == 0) return;               // every system finished in an earlier sweep
     if (p.fail && __ldg(p.nfail) == 0) return;    // the windowed pass solved every system
@@ -741,6 +753,8 @@ mp_update_kernel(MpArgs p)
 {
     __shared__ double sx[kMpTile + 4];
     __shared__ float s_red[kMpThreads / 32];
+    pdl_wait();
+    pdl_release();                                // one wave of persistent CTAs: the successor may queue now
     if (__ldg(p.live + p.sweep) == 0) return;      // every system finished in an earlier sweep
     const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
     for (int64_t blk = blockIdx.x; blk < p.m * tiles; blk += gridDim.x) {
@@ -832,9 +846,9 @@ cudaError_t launch_mp_pass_rpt(const MpPassArgs& p, int threads, int64_t blocks,
                                          (int)mp_pass_smem(kMpMaxRows));
     if (e != cudaSuccess) return e;
     blocks = std::min<int64_t>(blocks, mp_grid_cap((const void*)mp_pass_kernel<RPT>, threads, smem));
-    mp_pass_kernel<RPT><<<(unsigned)blocks, threads, smem, s>>>(p);
+    e = launch_dependent(mp_pass_kernel<RPT>, (unsigned)blocks, threads, smem, s, p);
     count_launch();
-    return cudaGetLastError();
+    return e;
 }
 
 }  // namespace
@@ -843,9 +857,9 @@ cudaError_t launch_mp_prep(const MpArgs& p, cudaStream_t s)
 {
     const int64_t nb = (p.n + 1) / 2;
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((p.m * nb + kMpThreads - 1) / kMpThreads, 152 * 16));
-    mp_prep_kernel<<<(unsigned)blocks, kMpThreads, 0, s>>>(p);
+    const cudaError_t e = launch_dependent(mp_prep_kernel, (unsigned)blocks, kMpThreads, 0, s, p);
     count_launch();
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s)
@@ -874,9 +888,9 @@ cudaError_t launch_mp_try(const MpPassArgs& p, cudaStream_t s)
                                          (int)mp_pass_smem(kMpMaxRows));
     if (e != cudaSuccess) return e;
     const int64_t blocks = std::min<int64_t>(items, mp_grid_cap((const void*)mp_try_kernel, kMpTryThreads, smem));
-    mp_try_kernel<<<(unsigned)blocks, kMpTryThreads, smem, s>>>(p);
+    e = launch_dependent(mp_try_kernel, (unsigned)blocks, kMpTryThreads, smem, s, p);
     count_launch();
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_mp_update(const MpArgs& p, cudaStream_t s)
@@ -885,9 +899,9 @@ cudaError_t launch_mp_update(const MpArgs& p, cudaStream_t s)
     // returns at once through the live count
     const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
     const int64_t blocks = std::min<int64_t>(p.m * tiles, mp_grid_cap((const void*)mp_update_kernel, kMpThreads, 0));
-    mp_update_kernel<<<(unsigned)blocks, kMpThreads, 0, s>>>(p);
+    const cudaError_t e = launch_dependent(mp_update_kernel, (unsigned)blocks, kMpThreads, 0, s, p);
     count_launch();
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_residual(const double* a, const double* b, const double* c, const double* d, const double* e,

@@ -58,6 +58,28 @@ struct MpPassArgs {
     int K, final_step, L, H, TRmax, sweep;
 };
 
+// Programmatic dependent launch: a kernel of the mixed solver may be
+// launched while its predecessor in the stream is still running; it waits
+// (griddepcontrol.wait) for the predecessor to complete and its writes to be
+// visible before touching memory.  Hides the launch gap between the many
+// short dependent kernels of a solve.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_dependent(void (*kernel)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t s,
+                             Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
+}
+
 cudaError_t launch_mp_prep(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s);
 cudaError_t launch_mp_try(const MpPassArgs& p, cudaStream_t s);
