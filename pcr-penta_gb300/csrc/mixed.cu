@@ -77,22 +77,20 @@ __device__ __forceinline__ int d_exponent(double v) {
 }
 
 // (float)(v * 2^-sh), rounded to nearest (ties away), flushing results below
-// FLT_MIN to zero and saturating to inf; integer arithmetic only.
+// FLT_MIN to zero and saturating to inf; integer arithmetic only, branch-free
+// (the special cases are selects).
 __device__ __forceinline__ float d2f_scaled(double v, int sh) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-    const unsigned sign = (unsigned)(bits >> 63) << 31;
-    const int E = (int)((bits >> 52) & 0x7FF);
-    if (E == 0) return __uint_as_float(sign);                      // zero / subnormal
-    if (E == 0x7FF) {                                               // inf / nan
-        const unsigned nan = (bits & 0xFFFFFFFFFFFFFULL) ? 0x400000u : 0u;
-        return __uint_as_float(sign | 0x7F800000u | nan);
-    }
-    const int F = E - sh - 1023 + 127;
-    if (F <= 0) return __uint_as_float(sign);
-    if (F >= 255) return __uint_as_float(sign | 0x7F800000u);
-    const unsigned long long mant = bits & 0xFFFFFFFFFFFFFULL;
-    unsigned u = ((unsigned)F << 23) + (unsigned)(mant >> 29) + (unsigned)((mant >> 28) & 1);
-    if (u >= 0x7F800000u) u = 0x7F800000u;
+    const unsigned hi = (unsigned)__double2hiint(v), lo = (unsigned)__double2loint(v);
+    const unsigned sign = hi & 0x80000000u;
+    const int E = (int)((hi >> 20) & 0x7FF);
+    const int F = E - sh - (1023 - 127);                        // biased FP32 exponent of the result
+    const unsigned mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);   // top 23 bits of the mantissa
+    unsigned u = ((unsigned)F << 23) + mant + ((lo >> 28) & 1u);
+    u = min(u, 0x7F800000u);                                     // rounded past the largest float: inf
+    u = F <= 0 ? 0u : u;
+    u = F >= 255 ? 0x7F800000u : u;
+    u = E == 0 ? 0u : u;                                         // zero and subnormal
+    u = E == 0x7FF ? (0x7F800000u | ((((hi & 0xFFFFFu) | lo) != 0u) ? 0x400000u : 0u)) : u;
     return __uint_as_float(sign | u);
 }
 
@@ -200,6 +198,47 @@ __device__ __forceinline__ BlockRow block_of(const PairRow& P, int64_t i0, int64
 // ---------------------------------------------------------------------------
 // prep: level-0 normalised block state and the first right-hand side
 // ---------------------------------------------------------------------------
+// One block row of the prep work: row scaling, FP32 blocks, diagonal inverse,
+// the normalised couplings and rhs.
+struct PrepRow { M2 L, U, Mi; float2 Y; };
+
+__device__ __forceinline__ PrepRow prep_row(const MpArgs& p, int64_t j, int64_t k)
+{
+    const PairRow P = load_pair(p, j * p.ss, 2 * k);
+    const BlockRow B = block_of(P, 2 * k, p.n);
+    PrepRow r;
+    r.Mi = minv(B.D);
+    r.L = mmul(r.Mi, B.L);
+    r.U = mmul(r.Mi, B.U);
+    const float y0 = d2f_scaled(P.y0, B.sh0);
+    const float y1 = 2 * k + 1 < p.n ? d2f_scaled(P.y1, B.sh1) : 0.0f;
+    r.Y = make_float2(fmaf(r.Mi.m0, y0, r.Mi.m1 * y1), fmaf(r.Mi.m2, y0, r.Mi.m3 * y1));
+    return r;
+}
+
+__device__ __forceinline__ void prep_store(const MpArgs& p, int64_t q, const PrepRow& r)
+{
+    p.S0[2 * q] = make_float4(r.L.m0, r.L.m1, r.L.m2, r.L.m3);
+    p.S0[2 * q + 1] = make_float4(r.U.m0, r.U.m1, r.U.m2, r.U.m3);
+    p.Mi[q] = make_float4(r.Mi.m0, r.Mi.m1, r.Mi.m2, r.Mi.m3);
+    p.R[0][q] = r.Y;
+}
+
+// per-system flags and norms of a solve
+__global__ void __launch_bounds__(kMpThreads)
+mp_init_kernel(MpArgs p)
+{
+    pdl_wait();
+    pdl_release();
+    const int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, st = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = t0; j < p.m; j += st) { p.fin[j] = 0; p.status[j] = 0; p.est[j] = 0.0f; p.fail[j] = 0; }
+    for (int64_t q = t0; q < (int64_t)kMpMaxPasses * p.m; q += st) p.trunc[q] = 0u;
+    for (int64_t q = t0; q < (int64_t)(p.max_sweeps + 1) * p.m; q += st) { p.ndx[q] = 0u; p.nx[q] = 0u; }
+    for (int64_t q = t0; q < (int64_t)p.max_sweeps * kMpMaxPasses * p.m; q += st) p.ndx_pre[q] = 0u;
+    if (t0 == 0) *p.nfail = 0;
+    for (int64_t q = t0; q <= p.max_sweeps; q += st) p.live[q] = (int)p.m;
+}
+
 __global__ void __launch_bounds__(kMpThreads)
 mp_prep_kernel(MpArgs p)
 {
@@ -209,31 +248,7 @@ mp_prep_kernel(MpArgs p)
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = q / nb, k = q - j * nb;
-        const int64_t base = j * p.ss;
-        const PairRow P = load_pair(p, base, 2 * k);
-        const BlockRow B = block_of(P, 2 * k, p.n);
-        const M2 Mi = minv(B.D);
-        const M2 L = mmul(Mi, B.L), U = mmul(Mi, B.U);
-        const float y0 = d2f_scaled(P.y0, B.sh0);
-        const float y1 = 2 * k + 1 < p.n ? d2f_scaled(P.y1, B.sh1) : 0.0f;
-        p.S0[2 * q] = make_float4(L.m0, L.m1, L.m2, L.m3);
-        p.S0[2 * q + 1] = make_float4(U.m0, U.m1, U.m2, U.m3);
-        p.Mi[q] = make_float4(Mi.m0, Mi.m1, Mi.m2, Mi.m3);
-        p.R[q] = make_float2(fmaf(Mi.m0, y0, Mi.m1 * y1), fmaf(Mi.m2, y0, Mi.m3 * y1));
-    }
-    if (blockIdx.x == 0) {
-        for (int64_t j = threadIdx.x; j < p.m; j += blockDim.x) {
-            p.fin[j] = 0; p.status[j] = 0; p.est[j] = 0.0f;
-        }
-        for (int64_t q = threadIdx.x; q < (int64_t)kMpMaxPasses * p.m; q += blockDim.x) p.trunc[q] = 0u;
-        for (int64_t q = threadIdx.x; q < (int64_t)(p.max_sweeps + 1) * p.m; q += blockDim.x) {
-            p.ndx[q] = 0u; p.nx[q] = 0u;
-        }
-        for (int64_t q = threadIdx.x; q < (int64_t)p.max_sweeps * kMpMaxPasses * p.m; q += blockDim.x)
-            p.ndx_pre[q] = 0u;
-        for (int64_t q = threadIdx.x; q < p.m; q += blockDim.x) p.fail[q] = 0;
-        if (threadIdx.x == 0) *p.nfail = 0;
-        for (int q = threadIdx.x; q <= p.max_sweeps; q += blockDim.x) p.live[q] = (int)p.m;
+        prep_store(p, q, prep_row(p, j, k));
     }
     pdl_release();                                // (multi-wave grid: release once this CTA is done)
 }
@@ -564,6 +579,126 @@ mp_try_kernel(MpPassArgs p)
     }
 }
 
+// Sweep 0 fused (prep, windowed cyclic reduction and the first refinement),
+// for windows that decouple (or hold the whole system).  Per window tile:
+//  1. FP64 bands and y of the tile's block rows -> row-scaled, normalised FP32
+//     blocks in shared memory; the window's own rows also go to S0, Mi and
+//     R[0] for the later sweeps and the general passes;
+//  2. cyclic reduction and back substitution (as mp_try_item): dx_0;
+//  3. x_0 = dx_0 on the window's rows and one block row each side (exact
+//     there: the valid region of the tile reaches 2 block rows beyond the
+//     window), written to X[0]; norms of dx_0 and x_0;
+//  4. r_0 = y - A x_0 in FP64 for the window's rows (bands and y read again,
+//     from L2), row-scaled and normalised -> R[1].
+// No decision is needed in sweep 0, so nothing waits for other windows.  A
+// window whose system stays coupled marks it and stops after step 1; the
+// general passes and the refinement kernel then take the whole system.
+__device__ __forceinline__ void first_item(const MpArgs& p, const MpWindows& g, int64_t item,
+                                           float4* sL, float4* sU, float2* sY)
+{
+    const int tid = threadIdx.x, bd = blockDim.x;
+    const int64_t n = p.n, nb = (n + 1) / 2;
+    const int64_t j = item / g.nwin, w = item - j * g.nwin;
+    const int64_t wlo = w * (int64_t)g.L, whi = min(wlo + (int64_t)g.L, nb);
+    const int64_t t0 = max(wlo - (int64_t)g.H, (int64_t)0), t1 = min(whi + (int64_t)g.H, nb);
+    const int TR = (int)(t1 - t0);
+    const bool whole = t0 == 0 && t1 == nb;
+
+    for (int k = tid; k < TR; k += bd) {
+        const int64_t kb = t0 + k;
+        const PrepRow r = prep_row(p, j, kb);
+        const int sk = swz(k);
+        sL[sk] = f4(r.L); sU[sk] = f4(r.U); sY[sk] = r.Y;
+        if (kb >= wlo && kb < whi) prep_store(p, j * nb + kb, r);
+    }
+    __syncthreads();
+    const int klo = (int)(wlo - t0), khi = (int)(whi - t0);
+    const int top = cr_reduce(sL, sU, sY, TR, whole ? 31 : g.K, klo, khi);
+    if (top < 0) {
+        if (tid == 0 && atomicOr(&p.fail[j], 1) == 0) atomicAdd(p.nfail, 1);
+        return;
+    }
+    cr_substitute(sL, sU, sY, TR, top);           // ends with a barrier: the L slots are free
+
+    // x_0 pairs, kept as double2 in the L slots for the residual's neighbours
+    double2* sX = reinterpret_cast<double2*>(sL);
+    const int xlo = max(klo - 1, 0), xhi = min(khi + 1, TR);
+    float dmax = 0.0f;
+    unsigned long long xbits = 0ull;
+    for (int k = xlo + tid; k < xhi; k += bd) {
+        const float2 v = sY[swz(k)];
+        const double2 x = make_double2(f2d(v.x), f2d(v.y));
+        sX[swz(k)] = x;
+        if (k >= klo && k < khi) {
+            const int64_t i0 = 2 * (t0 + k);
+            p.X[0][j * n + i0] = x.x;
+            dmax = fmaxf(dmax, fabsf(v.x));
+            xbits = max(xbits, (unsigned long long)__double_as_longlong(x.x) & 0x7FFFFFFFFFFFFFFFull);
+            if (i0 + 1 < n) {
+                p.X[0][j * n + i0 + 1] = x.y;
+                dmax = fmaxf(dmax, fabsf(v.y));
+                xbits = max(xbits, (unsigned long long)__double_as_longlong(x.y) & 0x7FFFFFFFFFFFFFFFull);
+            }
+        }
+    }
+    dmax = warp_max(dmax);
+    float xmax = warp_max(d2f_scaled(__longlong_as_double((long long)xbits), 0));
+    if ((tid & 31) == 0) {
+        atomic_max_pos(&p.ndx[j], dmax);
+        atomic_max_pos(&p.nx[j], xmax);
+    }
+    __syncthreads();
+
+    // r_0 = y - A x_0 on the window's block rows (FP64, same FMA order as the
+    // refinement kernel), row-scaled and normalised -> the rhs of sweep 1
+    for (int k = klo + tid; k < khi; k += bd) {
+        const int64_t kb = t0 + k, i0 = 2 * kb;
+        const PairRow P = load_pair(p, j * p.ss, i0);
+        const double2 xm = k > 0 ? sX[swz(k - 1)] : make_double2(0.0, 0.0);
+        const double2 xc = sX[swz(k)];
+        const double2 xp = k + 1 < TR ? sX[swz(k + 1)] : make_double2(0.0, 0.0);
+        double r0 = P.y0;                          // row i0: x_{i0-2..i0+2} = xm.x xm.y xc.x xc.y xp.x
+        r0 = fma(-P.c0, xc.x, r0);
+        if (i0 >= 2) r0 = fma(-P.a0, xm.x, r0);
+        if (i0 >= 1) r0 = fma(-P.b0, xm.y, r0);
+        if (i0 + 1 < n) r0 = fma(-P.d0, xc.y, r0);
+        if (i0 + 2 < n) r0 = fma(-P.e0, xp.x, r0);
+        float rf1 = 0.0f;                          // row i0+1 (the identity row of an odd system: 0)
+        if (i0 + 1 < n) {
+            const int64_t i1 = i0 + 1;             // x_{i1-2..i1+2} = xm.y xc.x xc.y xp.x xp.y
+            double r1 = P.y1;
+            r1 = fma(-P.c1, xc.y, r1);
+            if (i1 >= 2) r1 = fma(-P.a1, xm.y, r1);
+            r1 = fma(-P.b1, xc.x, r1);
+            if (i1 + 1 < n) r1 = fma(-P.d1, xp.x, r1);
+            if (i1 + 2 < n) r1 = fma(-P.e1, xp.y, r1);
+            rf1 = d2f_scaled(r1, d_exponent(P.c1));
+        }
+        const float rf0 = d2f_scaled(r0, d_exponent(P.c0));
+        const float4 Mi = p.Mi[j * nb + kb];
+        p.R[1][j * nb + kb] = make_float2(fmaf(Mi.x, rf0, Mi.y * rf1), fmaf(Mi.z, rf0, Mi.w * rf1));
+    }
+}
+
+// Persistent CTAs over the windows of all systems (40 KB tiles of 1024
+// block rows, or whole systems of up to 2048), 4 per SM at most.
+__global__ void __launch_bounds__(kMpTryThreads, 4)
+mp_first_kernel(MpArgs p, MpWindows g)
+{
+    extern __shared__ float4 fsm[];
+    pdl_wait();
+    pdl_release();                                // one wave of persistent CTAs: the successor may queue now
+    const int TRs = mp_pass_rows(g.TRmax);
+    float4* sL = fsm;
+    float4* sU = fsm + TRs;
+    float2* sY = reinterpret_cast<float2*>(fsm + 2 * TRs);
+    const int64_t items = p.m * g.nwin;
+    for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
+        first_item(p, g, it, sL, sU, sY);
+        __syncthreads();
+    }
+}
+
 // 4 CTAs per SM up to 4 rows per thread (64 registers, 40 KB of shared
 // memory each at 1024 block rows), 2 beyond
 template <int RPT>
@@ -744,7 +879,7 @@ __device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64
         // padded block, r = 0: its lane lies past t1 and keeps rf = 0)
         const float rf1 = __shfl_xor_sync(0xffffffffu, rf, 1);
         if (even && i < t1)
-            p.R[j * nb + (i >> 1)] = make_float2(fmaf(Mi.x, rf, Mi.y * rf1), fmaf(Mi.z, rf, Mi.w * rf1));
+            p.R[(s + 1) & 1][j * nb + (i >> 1)] = make_float2(fmaf(Mi.x, rf, Mi.y * rf1), fmaf(Mi.z, rf, Mi.w * rf1));
     }
 }
 
@@ -756,6 +891,7 @@ mp_update_kernel(MpArgs p)
     pdl_wait();
     pdl_release();                                // one wave of persistent CTAs: the successor may queue now
     if (__ldg(p.live + p.sweep) == 0) return;      // every system finished in an earlier sweep
+    if (p.first_fused && p.sweep == 0 && __ldg(p.nfail) == 0) return;   // the fused sweep 0 did it all
     const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
     for (int64_t blk = blockIdx.x; blk < p.m * tiles; blk += gridDim.x) {
         const int64_t j = blk / tiles;
@@ -763,6 +899,9 @@ mp_update_kernel(MpArgs p)
         // finished in an earlier sweep?  (fin is written during this kernel by
         // the tile-0 CTA for the current sweep; the other tiles must still run)
         const int f = p.fin[j];
+        // sweep 0 of a fused solve: only the systems the fused kernel left
+        // to the general passes
+        if (p.first_fused && p.sweep == 0 && !__ldg(p.fail + j)) continue;
         if (f == 0 || f > p.sweep) mp_update_tile(p, j, tile, sx, s_red);
         __syncthreads();
     }
@@ -852,6 +991,28 @@ cudaError_t launch_mp_pass_rpt(const MpPassArgs& p, int threads, int64_t blocks,
 }
 
 }  // namespace
+
+cudaError_t launch_mp_init(const MpArgs& p, cudaStream_t s)
+{
+    const cudaError_t e = launch_dependent(mp_init_kernel, 152u * 2, kMpThreads, 0, s, p);
+    count_launch();
+    return e;
+}
+
+cudaError_t launch_mp_first(const MpArgs& p, const MpWindows& g, cudaStream_t s)
+{
+    if (g.TRmax > kMpMaxRows) return cudaErrorInvalidValue;
+    const int64_t items = p.m * g.nwin;
+    if (items <= 0) return cudaSuccess;
+    const size_t smem = mp_pass_smem(g.TRmax);
+    cudaError_t e = cudaFuncSetAttribute(mp_first_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)mp_pass_smem(kMpMaxRows));
+    if (e != cudaSuccess) return e;
+    const int64_t blocks = std::min<int64_t>(items, mp_grid_cap((const void*)mp_first_kernel, kMpTryThreads, smem));
+    e = launch_dependent(mp_first_kernel, (unsigned)blocks, kMpTryThreads, smem, s, p, g);
+    count_launch();
+    return e;
+}
 
 cudaError_t launch_mp_prep(const MpArgs& p, cudaStream_t s)
 {

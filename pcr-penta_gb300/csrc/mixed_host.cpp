@@ -58,7 +58,7 @@ MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool 
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) / 256 * 256; return o; };
     L.S0 = take(2 * T * sizeof(float4));
-    L.R = take(T * sizeof(float2));
+    L.R = take(2 * T * sizeof(float2));
     L.Mi = take(T * sizeof(float4));
     L.P0 = pl.s1 > 0 ? take(2 * T * sizeof(float4) + T * sizeof(float2)) : 0;
     L.P1 = pl.npass > 1 ? take(2 * T * sizeof(float4) + T * sizeof(float2)) : 0;
@@ -114,7 +114,8 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     A.a = a; A.b = b; A.c = c; A.d = d; A.e = e; A.y = y;
     A.m = m; A.n = n; A.ss = ss; A.rs = rs;
     A.S0 = reinterpret_cast<float4*>(base + WL.S0);
-    A.R = reinterpret_cast<float2*>(base + WL.R);
+    A.R[0] = reinterpret_cast<float2*>(base + WL.R);
+    A.R[1] = A.R[0] + T;
     A.Mi = reinterpret_cast<float4*>(base + WL.Mi);
     A.dx = F(WL.dx);
     A.X[0] = reinterpret_cast<double*>(base + WL.X0);
@@ -135,30 +136,46 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
         for (const void* q : ptrs) if (reinterpret_cast<uintptr_t>(q) & 15) A.vec = 0;
     }
 
-    cudaError_t ce = launch_mp_prep(A, st);
-    if (ce != cudaSuccess) return cuda_error(ce, "mixed prep launch");
+    // Windows of the level-0 cyclic-reduction passes: whole systems when
+    // they fit one tile, else windows with a 2^(win+1) halo.
+    const bool windowed = pl.s1 > 0 && pl.win > 0;
+    MpWindows W{};
+    if (pl.s1 == 0) {
+        W.nwin = 1; W.L = (int)nb; W.H = 0; W.K = 31; W.TRmax = (int)nb;
+    } else if (windowed) {
+        W.H = 2 << pl.win; W.K = pl.win; W.L = kMpTryRows - 2 * W.H;
+        W.nwin = cdiv(nb, W.L);
+        W.TRmax = (int)std::min<int64_t>(W.L + 2 * W.H, nb);
+    }
+    // Sweep 0 fused into one kernel (prep, reduction, first refinement) when
+    // the level-0 pass is a cyclic-reduction one and a second sweep exists.
+    const bool fused = max_sweeps >= 2 && (pl.s1 == 0 || windowed);
+    A.first_fused = fused;
+
+    cudaError_t ce = launch_mp_init(A, st);
+    if (ce != cudaSuccess) return cuda_error(ce, "mixed init launch");
+    ce = fused ? launch_mp_first(A, W, st) : launch_mp_prep(A, st);
+    if (ce != cudaSuccess) return cuda_error(ce, fused ? "mixed first-sweep launch" : "mixed prep launch");
 
     float* P[2] = {pl.s1 > 0 ? F(WL.P0) : nullptr, pl.npass > 1 ? F(WL.P1) : nullptr};
     for (int s = 0; s < max_sweeps; s++) {
-        // FP32 block-PCR solve of the normalised system with rhs R
+        // FP32 block solve of the normalised system with rhs R[s & 1]
         MpPassArgs p{};
-        p.srcLU = A.S0; p.srcY = A.R;
+        p.srcLU = A.S0; p.srcY = A.R[s & 1];
         p.dx = A.dx; p.fin = A.fin; p.ndx = A.ndx; p.live = A.live + s;
         p.m = m; p.n = n; p.nb = nb; p.G = 1; p.sweep = s;
         unsigned* pre = A.ndx_pre + (size_t)s * kMpMaxPasses * m;
-        if (pl.s1 > 0 && pl.win > 0) {
+        if (windowed && !(fused && s == 0)) {
             // windowed cyclic reduction: solves the systems that decouple
             // within pl.win levels; the passes below take the others
             MpPassArgs t = p;
-            const int H = 2 << pl.win;
-            t.K = pl.win; t.H = H; t.L = kMpTryRows - 2 * H; t.final_step = 0;
-            t.nwin = cdiv(nb, t.L);
-            t.TRmax = (int)std::min<int64_t>(t.L + 2 * H, nb);
+            t.K = W.K; t.H = W.H; t.L = W.L; t.final_step = 0; t.nwin = W.nwin; t.TRmax = W.TRmax;
             t.fail = A.fail; t.nfail = A.nfail;
             ce = launch_mp_try(t, st);
             if (ce != cudaSuccess) return cuda_error(ce, "mixed windowed reduction launch");
-            p.fail = A.fail; p.nfail = A.nfail;
         }
+        // the passes below take only the systems a cyclic-reduction pass left coupled
+        if (windowed || (fused && s == 0)) { p.fail = A.fail; p.nfail = A.nfail; }
         int done = 0, pass = 0;
         while (done < pl.s1) {
             const int K = std::min(pl.fuse, pl.s1 - done);

@@ -17,7 +17,7 @@ struct MpArgs {
     double* y;                          // caller rhs in, solution out
     int64_t m, n, ss, rs;
     float4* S0;                         // level-0 normalised L,U: [2*q] = L, [2*q+1] = U, q < m*nb
-    float2* R;                          // normalised rhs Y of block row q
+    float2* R[2];                       // normalised rhs Y of block row q: sweep s reads R[s & 1]
     float4* Mi;                         // inverse of the row-scaled FP32 diagonal block of block row q
     float* dx;                          // FP32 correction, m*n (contiguous)
     double* X[2];                       // FP64 iterates, m*n each (contiguous): sweep s writes X[s&1]
@@ -34,6 +34,8 @@ struct MpArgs {
     int* nfail;                         // systems with fail set
     int sweep, max_sweeps, keep_x;
     int vec;                            // 1: all six caller arrays are 16-byte aligned (paired loads allowed)
+    int first_fused;                    // sweep 0 ran as mp_first_kernel (the refinement of sweep 0 only
+                                        // takes the systems it left to the general passes)
     float tol;
 };
 
@@ -80,6 +82,14 @@ cudaError_t launch_dependent(void (*kernel)(KArgs...), unsigned grid, unsigned b
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args&&>(args)...);
 }
 
+// Window geometry of the windowed passes (level 0).
+struct MpWindows {
+    int64_t nwin;                       // windows per system
+    int L, H, K, TRmax;                 // core rows, halo rows each side, levels (31: whole system), tile rows
+};
+
+cudaError_t launch_mp_init(const MpArgs& p, cudaStream_t s);
+cudaError_t launch_mp_first(const MpArgs& p, const MpWindows& g, cudaStream_t s);
 cudaError_t launch_mp_prep(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s);
 cudaError_t launch_mp_try(const MpPassArgs& p, cudaStream_t s);
