@@ -118,6 +118,26 @@ __device__ __forceinline__ float warp_max(float v) {
     return v;
 }
 
+// max |x| as the largest bit pattern with the sign cleared (non-negative
+// doubles order like their bits; a nan wins and poisons the norm)
+__device__ __forceinline__ unsigned long long absbits(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// x_s of rows [k0, k1) of system j (FP32 corrections d[k] of rows), with
+// the maxima of |dx| and |x| folded into dmax and xbits.
+__device__ __forceinline__ double x_update(const double* __restrict__ xsrc, int64_t xss, int64_t xrs,
+                                           double* __restrict__ xdst, int64_t dss, int64_t drs,
+                                           int64_t j, int64_t i, float d, float& dmax, unsigned long long& xbits)
+{
+    const double dd = f2d(d);
+    const double x = xsrc ? __dadd_rn(xsrc[j * xss + i * xrs], dd) : dd;
+    xdst[j * dss + i * drs] = x;
+    dmax = fmaxf(dmax, fabsf(d));
+    xbits = max(xbits, absbits(x));
+    return x;
+}
+
 // ---------------------------------------------------------------------------
 // 2x2 helpers (row-major m[0] m[1] / m[2] m[3])
 // ---------------------------------------------------------------------------
@@ -218,6 +238,7 @@ __device__ __forceinline__ PrepRow prep_row(const MpArgs& p, int64_t j, int64_t 
 
 __device__ __forceinline__ void prep_store(const MpArgs& p, int64_t q, const PrepRow& r)
 {
+    // (the rhs copy Yc is written by the callers, which have y in hand)
     p.S0[2 * q] = make_float4(r.L.m0, r.L.m1, r.L.m2, r.L.m3);
     p.S0[2 * q + 1] = make_float4(r.U.m0, r.U.m1, r.U.m2, r.U.m3);
     p.Mi[q] = make_float4(r.Mi.m0, r.Mi.m1, r.Mi.m2, r.Mi.m3);
@@ -249,6 +270,9 @@ mp_prep_kernel(MpArgs p)
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = q / nb, k = q - j * nb;
         prep_store(p, q, prep_row(p, j, k));
+        const int64_t i0 = 2 * k;
+        p.Yc[j * p.n + i0] = p.y[j * p.ss + i0 * p.rs];
+        if (i0 + 1 < p.n) p.Yc[j * p.n + i0 + 1] = p.y[j * p.ss + (i0 + 1) * p.rs];
     }
     pdl_release();                                // (multi-wave grid: release once this CTA is done)
 }
@@ -552,10 +576,26 @@ __device__ __forceinline__ void try_solve(const MpPassArgs& p, const TryTile& t,
         return;
     }
     cr_substitute(sL, sU, sY, t.TR, top);
-    // |dx| goes straight into the sweep's norm: if another window of the
-    // system fails, the general passes rewrite these rows with values equal
-    // to within the truncation, so the maximum stands either way
-    cr_store(p, t.j, 0, t.t0, (int)(t.wlo - t.t0), (int)(t.whi - t.t0), sY, &p.ndx[(int64_t)p.sweep * p.m + t.j]);
+    // x_s = x_{s-1} + dx_s on the window's rows, straight from the tile.  The
+    // norms go straight into the sweep's: if another window of the system
+    // fails, the general passes redo these rows with values equal to within
+    // the truncation, so the maxima stand either way.
+    const int klo = (int)(t.wlo - t.t0), khi = (int)(t.whi - t.t0);
+    float dmax = 0.0f;
+    unsigned long long xbits = 0ull;
+    for (int k = klo + threadIdx.x; k < khi; k += blockDim.x) {
+        const int64_t i0 = 2 * (t.t0 + k);
+        const float2 v = sY[swz(k)];
+        x_update(p.xsrc, p.xsrc_ss, p.xsrc_rs, p.xdst, p.xdst_ss, p.xdst_rs, t.j, i0, v.x, dmax, xbits);
+        if (i0 + 1 < p.n)
+            x_update(p.xsrc, p.xsrc_ss, p.xsrc_rs, p.xdst, p.xdst_ss, p.xdst_rs, t.j, i0 + 1, v.y, dmax, xbits);
+    }
+    dmax = warp_max(dmax);
+    const float xmax = warp_max(d2f_scaled(__longlong_as_double((long long)xbits), 0));
+    if ((threadIdx.x & 31) == 0) {
+        atomic_max_pos(&p.ndx[(int64_t)p.sweep * p.m + t.j], dmax);
+        atomic_max_pos(&p.nx[t.j], xmax);
+    }
 }
 
 // Persistent CTAs over the windows, 4 per SM (40 KB tiles of 1024 rows):
@@ -609,7 +649,12 @@ __device__ __forceinline__ void first_item(const MpArgs& p, const MpWindows& g, 
         const PrepRow r = prep_row(p, j, kb);
         const int sk = swz(k);
         sL[sk] = f4(r.L); sU[sk] = f4(r.U); sY[sk] = r.Y;
-        if (kb >= wlo && kb < whi) prep_store(p, j * nb + kb, r);
+        if (kb >= wlo && kb < whi) {
+            prep_store(p, j * nb + kb, r);
+            const int64_t i0 = 2 * kb;
+            p.Yc[j * n + i0] = p.y[j * p.ss + i0 * p.rs];
+            if (i0 + 1 < n) p.Yc[j * n + i0 + 1] = p.y[j * p.ss + (i0 + 1) * p.rs];
+        }
     }
     __syncthreads();
     const int klo = (int)(wlo - t0), khi = (int)(whi - t0);
@@ -631,11 +676,11 @@ __device__ __forceinline__ void first_item(const MpArgs& p, const MpWindows& g, 
         sX[swz(k)] = x;
         if (k >= klo && k < khi) {
             const int64_t i0 = 2 * (t0 + k);
-            p.X[0][j * n + i0] = x.x;
+            p.X0[j * n + i0] = x.x;
             dmax = fmaxf(dmax, fabsf(v.x));
             xbits = max(xbits, (unsigned long long)__double_as_longlong(x.x) & 0x7FFFFFFFFFFFFFFFull);
             if (i0 + 1 < n) {
-                p.X[0][j * n + i0 + 1] = x.y;
+                p.X0[j * n + i0 + 1] = x.y;
                 dmax = fmaxf(dmax, fabsf(v.y));
                 xbits = max(xbits, (unsigned long long)__double_as_longlong(x.y) & 0x7FFFFFFFFFFFFFFFull);
             }
@@ -740,46 +785,63 @@ mp_pass_kernel(MpPassArgs p)
 }
 
 // ---------------------------------------------------------------------------
-// refinement: x += dx (FP64), decide, and r = y - A x for the next sweep
+// refinement: x_s = x_{s-1} + dx_s (FP64), decide, r_s = y - A x_s
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64_t tile, double* sx, float* s_red)
+// Iterates: sweep 0 writes x_0 to X0 (workspace), every later sweep reads
+// x_{s-1} and writes x_s in the output (the caller's y, or Xout when the
+// report keeps y): a system that finishes in sweep s already holds its
+// answer there, and the rhs is read from the copy Yc.  The host passes each
+// sweep's source and destination (xsrc, xdst with their strides).
+
+// Systems whose dx came from the general passes (all of them when no cyclic-
+// reduction pass ran): x_s = x_{s-1} + dx_s and max |x_s|.
+__global__ void __launch_bounds__(kMpThreads)
+mp_xupdate_kernel(MpArgs p)
+{
+    __shared__ float s_red[kMpThreads / 32];
+    pdl_wait();
+    pdl_release();                                // one wave of persistent CTAs: the successor may queue now
+    const int s = p.sweep;
+    if (__ldg(p.live + s) == 0) return;           // every system finished in an earlier sweep
+    if (p.cr_mode && __ldg(p.nfail) == 0) return; // the cyclic-reduction passes updated every system
+    constexpr int XT = 4 * kMpThreads;            // rows per tile
+    const int64_t n = p.n, tiles = (n + XT - 1) / XT;
+    for (int64_t blk = blockIdx.x; blk < p.m * tiles; blk += gridDim.x) {
+        const int64_t j = blk / tiles, t0 = (blk - j * tiles) * XT;
+        if (__ldg(p.fin + j) != 0) continue;
+        if (p.cr_mode && !__ldg(p.fail + j)) continue;
+        float dmax = 0.0f;
+        unsigned long long xbits = 0ull;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int64_t i = t0 + threadIdx.x + u * kMpThreads;
+            if (i < n) x_update(p.xsrc, p.xsrc_ss, p.xsrc_rs, p.xdst, p.xdst_ss, p.xdst_rs, j, i, p.dx[j * n + i],
+                                dmax, xbits);
+        }
+        float xmax = warp_max(d2f_scaled(__longlong_as_double((long long)xbits), 0));
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = xmax;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float v = 0.0f;
+            for (int w = 0; w < kMpThreads / 32; w++) v = fmaxf(v, s_red[w]);
+            atomic_max_pos(&p.nx[(int64_t)s * p.m + j], v);
+        }
+        __syncthreads();
+    }
+}
+
+// Per-system decision after sweep s from the norms of this sweep and the last.
+struct UpDecision { bool done, last; float est; };
+
+__device__ __forceinline__ UpDecision up_decide(const MpArgs& p, int64_t j)
 {
     const int s = p.sweep;
-    const int tid = threadIdx.x;
-    const int64_t n = p.n;
-    constexpr int XR = kMpTile / kMpThreads;             // rows per thread
-
-    // Rows t0 + tid + u*kMpThreads of the tile [t0, t1); threads 0-3 also take
-    // the halo rows t0-2, t0-1, t1, t1+1 of x, recomputed bit-identically by
-    // the neighbouring tiles.  The x loads go first, then the norms the
-    // decision needs, then the bands: one memory round trip in sweep 0 (no
-    // decision to wait for) and in a last sweep (no bands to read).
-    const int64_t t0 = tile * kMpTile;
-    const int64_t t1 = min(t0 + kMpTile, n);
-    const int64_t ih = tid < 2 ? t0 - 2 + tid : t1 + tid - 2;          // halo row of threads 0-3
-    const bool halo = tid < 4 && ih >= 0 && ih < n;
-    // x_{s-1} comes from the other ping-pong buffer: neighbouring tiles read
-    // their halo rows from it while this tile writes x_s
-    const double* __restrict__ xprev = p.X[(s + 1) & 1] + j * n;
-    const float* __restrict__ dxs = p.dx + j * n;
-    float dv[XR], dvh = 0.0f;
-    double xv[XR], xvh = 0.0;
-#pragma unroll
-    for (int u = 0; u < XR; u++) {
-        const int64_t i = t0 + tid + u * kMpThreads;
-        dv[u] = 0.0f; xv[u] = 0.0;
-        if (i < t1) { dv[u] = dxs[i]; if (s > 0) xv[u] = xprev[i]; }
-    }
-    if (halo) { dvh = dxs[ih]; if (s > 0) xvh = xprev[ih]; }
-
-    // per-system decision from the norms the previous kernels left behind
-    bool done = false;
-    float est = 0.0f;
+    UpDecision D{false, false, 0.0f};
     if (s >= 1) {
         const float nd = __uint_as_float(p.ndx[(int64_t)s * p.m + j]);
         const float ndp = __uint_as_float(p.ndx[(int64_t)(s - 1) * p.m + j]);
         const float nxp = __uint_as_float(p.nx[(int64_t)(s - 1) * p.m + j]);
-        if (nd == 0.0f) { done = true; est = 0.0f; }
+        if (nd == 0.0f) D.done = true;
         else if (ndp > 0.0f) {
             // Two ways to be done.  (1) The correction itself is below tol/2:
             // x_{s-1} was off by about |dx_s|, and applying dx_s leaves at most
@@ -791,63 +853,67 @@ __device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64
             const float rel = nd / fmaxf(nxp, FLT_MIN);
             const float rho = nd / ndp;
             const float contr = rho < 0.5f ? 2.0f * rho / (1.0f - rho) * rel : rel;
-            est = fminf(rel, contr);
-            done = rel <= 0.5f * p.tol || (rho < 0.5f && contr <= p.tol);
+            D.est = fminf(rel, contr);
+            D.done = rel <= 0.5f * p.tol || (rho < 0.5f && contr <= p.tol);
         }
     }
-    const bool last = done || s == p.max_sweeps - 1;
-    const bool to_user = last && !p.keep_x;
+    D.last = D.done || s == p.max_sweeps - 1;
+    return D;
+}
 
-    // bands and y of this thread's rows, for the residual (not read in a last sweep)
-    const int64_t ybase = j * p.ss;
+// One thread per system: a system that is done (or out of sweeps) finishes in
+// sweep s; its answer is already in the output.
+__global__ void __launch_bounds__(kMpThreads)
+mp_decide_kernel(MpArgs p)
+{
+    pdl_wait();
+    pdl_release();
+    const int s = p.sweep;
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    bool finish = false;
+    if (j < p.m && p.fin[j] == 0) {
+        const UpDecision D = up_decide(p, j);
+        if (D.last) {
+            p.est[j] = D.est;
+            p.status[j] = D.done ? 1 : 2;         // 2: stopped at max_sweeps
+            p.fin[j] = s + 1;
+            finish = true;
+        }
+    }
+    const int cnt = __syncthreads_count(finish);
+    if (threadIdx.x == 0 && cnt > 0)
+        for (int s2 = s + 1; s2 <= p.max_sweeps; s2++) atomicSub(&p.live[s2], cnt);
+}
+
+// r_s = y - A x_s (FP64, FMA chain) for the systems still running, row-scaled
+// to FP32 by the power of two of the main diagonal; the odd row of a block
+// row reaches the even lane by a shuffle, which normalises the pair by the
+// block's diagonal inverse -> R[(s+1) & 1], the rhs of sweep s+1.
+__device__ __forceinline__ void residual_tile(const MpArgs& p, int64_t j, int64_t tile, double* sx)
+{
+    const int s = p.sweep, tid = threadIdx.x;
+    const int64_t n = p.n;
+    constexpr int XR = kMpTile / kMpThreads;             // rows per thread
+    const int64_t t0 = tile * kMpTile, t1 = min(t0 + kMpTile, n);
+    const int64_t ih = tid < 2 ? t0 - 2 + tid : t1 + tid - 2;          // halo row of threads 0-3
+    const bool halo = tid < 4 && ih >= 0 && ih < n;
+    const double* __restrict__ x = p.xdst;                // x_s, written by this sweep's earlier kernels
+    const int64_t xs = j * p.xdst_ss;
     double ba[XR], bb[XR], bc[XR], bd[XR], be[XR], by[XR];
 #pragma unroll
     for (int u = 0; u < XR; u++) {
         const int64_t i = t0 + tid + u * kMpThreads;
         ba[u] = 0.0; bb[u] = 0.0; bc[u] = 1.0; bd[u] = 0.0; be[u] = 0.0; by[u] = 0.0;
-        if (!last && i < t1) {
-            const int64_t g = ybase + i * p.rs;
-            ba[u] = p.a[g]; bb[u] = p.b[g]; bc[u] = p.c[g]; bd[u] = p.d[g]; be[u] = p.e[g]; by[u] = p.y[g];
-        }
-    }
-
-    // max |x| as the largest bit pattern with the sign cleared (non-negative
-    // doubles order like their bits; a nan wins and poisons the norm)
-    unsigned long long xbits = 0ull;
-#pragma unroll
-    for (int u = 0; u < XR; u++) {
-        const int64_t i = t0 + tid + u * kMpThreads;
         if (i < t1) {
-            const double xi = s == 0 ? f2d(dv[u]) : __dadd_rn(xv[u], f2d(dv[u]));
-            sx[tid + u * kMpThreads + 2] = xi;
-            if (to_user) p.y[ybase + i * p.rs] = xi;
-            else if (last) p.Xout[j * n + i] = xi;
-            else p.X[s & 1][j * n + i] = xi;
-            xbits = max(xbits, (unsigned long long)__double_as_longlong(xi) & 0x7FFFFFFFFFFFFFFFull);
+            const int64_t g = j * p.ss + i * p.rs;
+            ba[u] = p.a[g]; bb[u] = p.b[g]; bc[u] = p.c[g]; bd[u] = p.d[g]; be[u] = p.e[g];
+            by[u] = p.Yc[j * n + i];
+            sx[tid + u * kMpThreads + 2] = x[xs + i * p.xdst_rs];
         }
     }
-    if (halo) sx[ih - t0 + 2] = s == 0 ? f2d(dvh) : __dadd_rn(xvh, f2d(dvh));
-    float xmax = d2f_scaled(__longlong_as_double((long long)xbits), 0);   // in FP32: it only feeds the estimate
-    xmax = warp_max(xmax);
-    if ((tid & 31) == 0) s_red[tid >> 5] = xmax;
+    if (halo) sx[ih - t0 + 2] = x[xs + ih * p.xdst_rs];
     __syncthreads();
-    if (tid == 0) {
-        float v = 0.0f;
-        for (int w = 0; w < (int)(blockDim.x / 32); w++) v = fmaxf(v, s_red[w]);
-        atomic_max_pos(&p.nx[(int64_t)s * p.m + j], v);
-        if (tile == 0 && last) {
-            p.est[j] = est;
-            p.status[j] = done ? 1 : 2;      // 2: stopped at max_sweeps
-            p.fin[j] = s + 1;
-            for (int s2 = s + 1; s2 <= p.max_sweeps; s2++) atomicSub(&p.live[s2], 1);
-        }
-    }
-    if (last) return;
 
-    // residual r = y - A x (FP64, FMA chain), row-scaled to FP32 by the power
-    // of two of its main diagonal; the odd row of a block row reaches the even
-    // lane by a shuffle, which normalises the pair by the block's diagonal
-    // inverse (left by the prep kernel) -> the next FP32 rhs
     const int64_t nb = (n + 1) / 2;
     const bool interior = t0 >= 2 && t1 + 2 <= n;          // no band slot of the tile falls outside the system
 #pragma unroll
@@ -883,26 +949,23 @@ __device__ __forceinline__ void mp_update_tile(const MpArgs& p, int64_t j, int64
     }
 }
 
+// 5 CTAs per SM (at most 51 registers)
 __global__ void __launch_bounds__(kMpThreads, 5)
-mp_update_kernel(MpArgs p)
+mp_residual_kernel(MpArgs p)
 {
     __shared__ double sx[kMpTile + 4];
-    __shared__ float s_red[kMpThreads / 32];
     pdl_wait();
     pdl_release();                                // one wave of persistent CTAs: the successor may queue now
-    if (__ldg(p.live + p.sweep) == 0) return;      // every system finished in an earlier sweep
-    if (p.first_fused && p.sweep == 0 && __ldg(p.nfail) == 0) return;   // the fused sweep 0 did it all
+    const int s = p.sweep;
+    if (__ldg(p.live + s + 1) == 0) return;       // every system has finished
+    const bool fused0 = p.first_fused && s == 0;  // the fused sweep 0 formed r_0 of the systems it solved
+    if (fused0 && __ldg(p.nfail) == 0) return;
     const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
     for (int64_t blk = blockIdx.x; blk < p.m * tiles; blk += gridDim.x) {
         const int64_t j = blk / tiles;
-        const int64_t tile = blk - j * tiles;
-        // finished in an earlier sweep?  (fin is written during this kernel by
-        // the tile-0 CTA for the current sweep; the other tiles must still run)
-        const int f = p.fin[j];
-        // sweep 0 of a fused solve: only the systems the fused kernel left
-        // to the general passes
-        if (p.first_fused && p.sweep == 0 && !__ldg(p.fail + j)) continue;
-        if (f == 0 || f > p.sweep) mp_update_tile(p, j, tile, sx, s_red);
+        if (__ldg(p.fin + j) != 0) continue;
+        if (fused0 && !__ldg(p.fail + j)) continue;
+        residual_tile(p, j, blk - j * tiles, sx);
         __syncthreads();
     }
 }
@@ -1054,13 +1117,30 @@ cudaError_t launch_mp_try(const MpPassArgs& p, cudaStream_t s)
     return e;
 }
 
-cudaError_t launch_mp_update(const MpArgs& p, cudaStream_t s)
+cudaError_t launch_mp_xupdate(const MpArgs& p, cudaStream_t s)
 {
-    // one wave of CTAs striding over the tiles: a sweep with nothing left
-    // returns at once through the live count
+    const int64_t tiles = (p.n + 4 * kMpThreads - 1) / (4 * kMpThreads);
+    const int64_t blocks = std::min<int64_t>(p.m * tiles, mp_grid_cap((const void*)mp_xupdate_kernel, kMpThreads, 0));
+    const cudaError_t e = launch_dependent(mp_xupdate_kernel, (unsigned)blocks, kMpThreads, 0, s, p);
+    count_launch();
+    return e;
+}
+
+cudaError_t launch_mp_decide(const MpArgs& p, cudaStream_t s)
+{
+    const int64_t blocks = (p.m + kMpThreads - 1) / kMpThreads;
+    const cudaError_t e = launch_dependent(mp_decide_kernel, (unsigned)blocks, kMpThreads, 0, s, p);
+    count_launch();
+    return e;
+}
+
+cudaError_t launch_mp_residual(const MpArgs& p, cudaStream_t s)
+{
+    // one wave of CTAs striding over the tiles: a sweep after which every
+    // system has finished returns at once through the live count
     const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
-    const int64_t blocks = std::min<int64_t>(p.m * tiles, mp_grid_cap((const void*)mp_update_kernel, kMpThreads, 0));
-    const cudaError_t e = launch_dependent(mp_update_kernel, (unsigned)blocks, kMpThreads, 0, s, p);
+    const int64_t blocks = std::min<int64_t>(p.m * tiles, mp_grid_cap((const void*)mp_residual_kernel, kMpThreads, 0));
+    const cudaError_t e = launch_dependent(mp_residual_kernel, (unsigned)blocks, kMpThreads, 0, s, p);
     count_launch();
     return e;
 }

@@ -47,7 +47,7 @@ MpPlan mp_plan(int64_t nb, const pcrp_opts* o)
 }
 
 struct MpLayout {
-    size_t S0, R, Mi, P0, P1, dx, X0, X1, Xout, ndx, nx, fin, status, est, trunc, ndx_pre, live, fail, nfail, rbuf, rn,
+    size_t S0, R, Mi, P0, P1, dx, X0, Yc, Xout, ndx, nx, fin, status, est, trunc, ndx_pre, live, fail, nfail, rbuf, rn,
         total;
 };
 
@@ -64,7 +64,7 @@ MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool 
     L.P1 = pl.npass > 1 ? take(2 * T * sizeof(float4) + T * sizeof(float2)) : 0;
     L.dx = take((size_t)m * n * sizeof(float));
     L.X0 = take((size_t)m * n * sizeof(double));
-    L.X1 = take((size_t)m * n * sizeof(double));
+    L.Yc = take((size_t)m * n * sizeof(double));
     L.Xout = info ? take((size_t)m * n * sizeof(double)) : 0;
     L.ndx = take((size_t)(max_sweeps + 1) * m * sizeof(unsigned));
     L.nx = take((size_t)(max_sweeps + 1) * m * sizeof(unsigned));
@@ -118,8 +118,8 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     A.R[1] = A.R[0] + T;
     A.Mi = reinterpret_cast<float4*>(base + WL.Mi);
     A.dx = F(WL.dx);
-    A.X[0] = reinterpret_cast<double*>(base + WL.X0);
-    A.X[1] = reinterpret_cast<double*>(base + WL.X1);
+    A.X0 = reinterpret_cast<double*>(base + WL.X0);
+    A.Yc = reinterpret_cast<double*>(base + WL.Yc);
     A.Xout = keep_x ? reinterpret_cast<double*>(base + WL.Xout) : nullptr;
     A.ndx = U(WL.ndx); A.nx = U(WL.nx);
     A.fin = reinterpret_cast<int*>(base + WL.fin);
@@ -139,6 +139,7 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     // Windows of the level-0 cyclic-reduction passes: whole systems when
     // they fit one tile, else windows with a 2^(win+1) halo.
     const bool windowed = pl.s1 > 0 && pl.win > 0;
+    const bool cr_mode = pl.s1 == 0 || windowed;
     MpWindows W{};
     if (pl.s1 == 0) {
         W.nwin = 1; W.L = (int)nb; W.H = 0; W.K = 31; W.TRmax = (int)nb;
@@ -147,10 +148,15 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
         W.nwin = cdiv(nb, W.L);
         W.TRmax = (int)std::min<int64_t>(W.L + 2 * W.H, nb);
     }
-    // Sweep 0 fused into one kernel (prep, reduction, first refinement) when
-    // the level-0 pass is a cyclic-reduction one and a second sweep exists.
-    const bool fused = max_sweeps >= 2 && (pl.s1 == 0 || windowed);
+    // Sweep 0 fused into one kernel (prep, reduction, x_0, r_0) when the
+    // level-0 pass is a cyclic-reduction one and a second sweep exists.
+    const bool fused = max_sweeps >= 2 && cr_mode;
     A.first_fused = fused;
+    A.cr_mode = cr_mode;
+    // Iterates: x_0 in X0 when more sweeps follow, every later x_s in the
+    // output (y, or Xout when y must keep the rhs for the report).
+    double* xout = keep_x ? A.Xout : y;
+    const int64_t oss = keep_x ? n : ss, ors = keep_x ? 1 : rs;
 
     cudaError_t ce = launch_mp_init(A, st);
     if (ce != cudaSuccess) return cuda_error(ce, "mixed init launch");
@@ -159,23 +165,33 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
 
     float* P[2] = {pl.s1 > 0 ? F(WL.P0) : nullptr, pl.npass > 1 ? F(WL.P1) : nullptr};
     for (int s = 0; s < max_sweeps; s++) {
+        A.sweep = s;
+        if (s == 0) { A.xsrc = nullptr; A.xsrc_ss = 0; A.xsrc_rs = 0; }
+        else if (s == 1) { A.xsrc = A.X0; A.xsrc_ss = n; A.xsrc_rs = 1; }
+        else { A.xsrc = xout; A.xsrc_ss = oss; A.xsrc_rs = ors; }
+        if (s == 0 && max_sweeps >= 2) { A.xdst = A.X0; A.xdst_ss = n; A.xdst_rs = 1; }
+        else { A.xdst = xout; A.xdst_ss = oss; A.xdst_rs = ors; }
+
         // FP32 block solve of the normalised system with rhs R[s & 1]
         MpPassArgs p{};
         p.srcLU = A.S0; p.srcY = A.R[s & 1];
         p.dx = A.dx; p.fin = A.fin; p.ndx = A.ndx; p.live = A.live + s;
         p.m = m; p.n = n; p.nb = nb; p.G = 1; p.sweep = s;
         unsigned* pre = A.ndx_pre + (size_t)s * kMpMaxPasses * m;
-        if (windowed && !(fused && s == 0)) {
-            // windowed cyclic reduction: solves the systems that decouple
-            // within pl.win levels; the passes below take the others
+        if (cr_mode && !(fused && s == 0)) {
+            // cyclic reduction of whole systems or of windows that decouple
+            // within pl.win levels, with x_s = x_{s-1} + dx_s; the passes
+            // below take the systems it leaves coupled
             MpPassArgs t = p;
             t.K = W.K; t.H = W.H; t.L = W.L; t.final_step = 0; t.nwin = W.nwin; t.TRmax = W.TRmax;
             t.fail = A.fail; t.nfail = A.nfail;
+            t.xsrc = A.xsrc; t.xsrc_ss = A.xsrc_ss; t.xsrc_rs = A.xsrc_rs;
+            t.xdst = A.xdst; t.xdst_ss = A.xdst_ss; t.xdst_rs = A.xdst_rs;
+            t.nx = A.nx + (size_t)s * m;
             ce = launch_mp_try(t, st);
-            if (ce != cudaSuccess) return cuda_error(ce, "mixed windowed reduction launch");
+            if (ce != cudaSuccess) return cuda_error(ce, "mixed cyclic-reduction launch");
         }
-        // the passes below take only the systems a cyclic-reduction pass left coupled
-        if (windowed || (fused && s == 0)) { p.fail = A.fail; p.nfail = A.nfail; }
+        if (cr_mode) { p.fail = A.fail; p.nfail = A.nfail; }
         int done = 0, pass = 0;
         while (done < pl.s1) {
             const int K = std::min(pl.fuse, pl.s1 - done);
@@ -197,19 +213,24 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
             p.srcLU = p.dstLU; p.srcY = p.dstY;
             p.G <<= K; done += K; pass++;
         }
-        const int64_t nrmax = cdiv(nb, p.G);
-        int Kf = 0;
-        while ((int64_t(1) << Kf) < nrmax) Kf++;
-        p.K = Kf; p.H = 0; p.L = (int)nrmax; p.final_step = 1; p.nwin = 1; p.TRmax = (int)nrmax;
-        p.trunc_in = pass > 0 ? A.trunc + (pass - 1) * m : nullptr;
-        p.trunc_out = nullptr;
-        p.ndx_pre_in = pass > 0 ? pre + (pass - 1) * m : nullptr;
-        p.ndx_pre_out = nullptr;
-        ce = launch_mp_pass(p, st);
-        if (ce != cudaSuccess) return cuda_error(ce, "mixed shared-memory pass launch");
-        // FP64 update, stopping decision, next residual
-        A.sweep = s;
-        ce = launch_mp_update(A, st);
+        if (!(cr_mode && pl.s1 == 0)) {            // whole systems never leave the cyclic-reduction pass
+            const int64_t nrmax = cdiv(nb, p.G);
+            int Kf = 0;
+            while ((int64_t(1) << Kf) < nrmax) Kf++;
+            p.K = Kf; p.H = 0; p.L = (int)nrmax; p.final_step = 1; p.nwin = 1; p.TRmax = (int)nrmax;
+            p.trunc_in = pass > 0 ? A.trunc + (pass - 1) * m : nullptr;
+            p.trunc_out = nullptr;
+            p.ndx_pre_in = pass > 0 ? pre + (pass - 1) * m : nullptr;
+            p.ndx_pre_out = nullptr;
+            ce = launch_mp_pass(p, st);
+            if (ce != cudaSuccess) return cuda_error(ce, "mixed shared-memory pass launch");
+            // x_s of the systems the passes solved
+            ce = launch_mp_xupdate(A, st);
+            if (ce != cudaSuccess) return cuda_error(ce, "mixed update launch");
+        }
+        // stopping decision, then the next rhs of the systems still running
+        ce = launch_mp_decide(A, st);
+        if (ce == cudaSuccess && s + 1 < max_sweeps) ce = launch_mp_residual(A, st);
         if (ce != cudaSuccess) return cuda_error(ce, "mixed refinement launch");
     }
     if (out) *out = A;

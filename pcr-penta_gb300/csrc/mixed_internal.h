@@ -20,8 +20,13 @@ struct MpArgs {
     float2* R[2];                       // normalised rhs Y of block row q: sweep s reads R[s & 1]
     float4* Mi;                         // inverse of the row-scaled FP32 diagonal block of block row q
     float* dx;                          // FP32 correction, m*n (contiguous)
-    double* X[2];                       // FP64 iterates, m*n each (contiguous): sweep s writes X[s&1]
-    double* Xout;                       // final iterate when the caller asked for a report (keep_x)
+    double* X0;                         // x_0, m*n contiguous (sweep 0 of a multi-sweep solve)
+    double* Xout;                       // iterates when the caller asked for a report (keep_x), else y
+    double* Yc;                         // copy of the rhs, m*n contiguous (y may hold the iterate)
+    const double* xsrc;                 // this sweep's x_{s-1} (null in sweep 0) ...
+    int64_t xsrc_ss, xsrc_rs;           //   ... and its system / row strides
+    double* xdst;                       // this sweep's x_s ...
+    int64_t xdst_ss, xdst_rs;
     unsigned* ndx;                      // [(max_sweeps+1) x m] max |dx| per sweep (float bits)
     unsigned* nx;                       // [(max_sweeps+1) x m] max |x| per sweep
     int* fin;                           // per system: 0 running, else the sweep it finished in, plus 1
@@ -36,6 +41,7 @@ struct MpArgs {
     int vec;                            // 1: all six caller arrays are 16-byte aligned (paired loads allowed)
     int first_fused;                    // sweep 0 ran as mp_first_kernel (the refinement of sweep 0 only
                                         // takes the systems it left to the general passes)
+    int cr_mode;                        // a cyclic-reduction pass updates x of the systems it solves
     float tol;
 };
 
@@ -56,6 +62,11 @@ struct MpPassArgs {
     int* fail;                          // per system: the windowed cyclic-reduction pass did not decouple it
                                         // (null: no such pass; general passes then run for every system)
     int* nfail;                         // number of systems with fail set
+    const double* xsrc;                 // cyclic-reduction passes: x_{s-1} (null in sweep 0) ...
+    int64_t xsrc_ss, xsrc_rs;
+    double* xdst;                       //   ... and x_s = x_{s-1} + dx_s (null: write dx instead)
+    int64_t xdst_ss, xdst_rs;
+    unsigned* nx;                       //   ... and max |x_s|
     int64_t m, n, nb, G, nwin;
     int K, final_step, L, H, TRmax, sweep;
 };
@@ -93,7 +104,9 @@ cudaError_t launch_mp_first(const MpArgs& p, const MpWindows& g, cudaStream_t s)
 cudaError_t launch_mp_prep(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s);
 cudaError_t launch_mp_try(const MpPassArgs& p, cudaStream_t s);
-cudaError_t launch_mp_update(const MpArgs& p, cudaStream_t s);
+cudaError_t launch_mp_xupdate(const MpArgs& p, cudaStream_t s);
+cudaError_t launch_mp_decide(const MpArgs& p, cudaStream_t s);
+cudaError_t launch_mp_residual(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_residual(const double* a, const double* b, const double* c, const double* d, const double* e,
                             const double* y, const double* x, double* r, int64_t m, int64_t n, int64_t ss,
                             int64_t rs, int64_t xss, int64_t xrs, cudaStream_t s);
