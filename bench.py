@@ -36,6 +36,26 @@ METRIC = "Gunknowns/s, % of 8 TB/s HBM; FP32+IR vs FP64 PCR at ≤1e-12 fwd err"
 UNIT = "Gunknowns/s"
 BYTES_PER_UNKNOWN = 56          # 5 FP64 bands + FP64 rhs read once, FP64 x written once
 
+
+def ref_strides(n: int) -> int:
+    """Strides PCR-Penta runs on n rows (main.cu:38-39): log2 n for powers of
+    two, ceil(log2 n) - 1 otherwise."""
+    if n <= 1:
+        return 0
+    lg = (n - 1).bit_length()
+    return lg if (1 << lg) == n else lg - 1
+
+
+def fp64_ops(n: int):
+    """FP64 operations per unknown of the faithful solve (the reference's
+    arithmetic, division pairs shared as in the kernels): per row and stride 4
+    IEEE divisions and 36 rounded products or sums; then x = y/c for powers of
+    two, or the 2x2 pairs (per row: 1 division, 3 products/sums)."""
+    s = ref_strides(n)
+    if n >= 2 and (1 << s) == n:
+        return 36 * s, 4 * s + 1
+    return 36 * s + 3, 4 * s + 1
+
 CONFIGS = {
     "c0": dict(m=1024, n=512, kind=0, name="plain FP64 PCR, shared-memory path, m=1024 n=512"),
     "c1": dict(m=256, n=65536, kind=0, name="plain FP64 PCR, global tile-splitting path, m=256 n=65536"),
@@ -204,19 +224,34 @@ def run_ours(args, world, rank, local, pg):
     torch.cuda.synchronize(dev)
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
+    # inputs that fit in L2 are flushed between timed steps (a write larger
+    # than L2), each step then timed alone
+    l2 = torch.cuda.get_device_properties(dev).L2_cache_size
+    small = 48 * m * n < 2 * l2
+    flush = torch.empty(2 * l2 // 4 + 1024, dtype=torch.float32, device=dev) if small else None
+    step_ms = []
     with ClockSampler(local) as clk:
         time.sleep(0.3)
         with torch.cuda.stream(stream):
-            ev0.record(stream)
-            for _ in range(args.steps):
-                step()
-            ev1.record(stream)
+            if small:
+                for _ in range(args.steps):
+                    flush.zero_()
+                    ev0.record(stream)
+                    step()
+                    ev1.record(stream)
+                    ev1.synchronize()
+                    step_ms.append(ev0.elapsed_time(ev1))
+            else:
+                ev0.record(stream)
+                for _ in range(args.steps):
+                    step()
+                ev1.record(stream)
         ev1.synchronize()
         time.sleep(0.1)
     torch.cuda.synchronize(dev)
     barrier()
     launches = pcrp.kernel_launches() - launches0
-    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = sum(step_ms) / args.steps if small else ev0.elapsed_time(ev1) / args.steps
     if pg is not None:
         t = torch.tensor([ms], dtype=torch.float64, device=dev if pg.get_backend() == "nccl" else "cpu")
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
@@ -230,6 +265,8 @@ def run_ours(args, world, rank, local, pg):
     with torch.cuda.stream(stream):
         for _ in range(max(3, args.steps)):
             arrs[5].copy_(rhs, non_blocking=True)
+            if small:
+                flush.zero_()
             ek0.record(stream)
             solve()
             ek1.record(stream)
@@ -237,6 +274,19 @@ def run_ours(args, world, rank, local, pg):
             kms.append(ek0.elapsed_time(ek1))
     kms_med = statistics.median(kms)
     achieved = BYTES_PER_UNKNOWN * m * n / (kms_med * 1e-3) / 1e9
+
+    # FP64-pipe roofline of the faithful path: its FP64 operations at this
+    # GPU's measured DFMA and division rates, against the kernel time
+    fp64_roof = None
+    if args.solver == "f64":
+        dfma, ddiv = pcrp.measure_fp64(stream)
+        ops, divs = fp64_ops(n)
+        t_peak = m * n * (ops / dfma + divs / ddiv)
+        fp64_roof = {"bound": "fp64", "ops_per_unknown": ops, "divisions_per_unknown": divs,
+                     "dfma_per_s": dfma, "ddiv_per_s": ddiv,
+                     "ms_at_peak": t_peak * 1e3, "frac": t_peak / (kms_med * 1e-3),
+                     "note": "FP64 products/sums at the measured DFMA rate plus IEEE divisions at the "
+                             "measured division rate (pcrp_measure_fp64), over the solve's kernel time"}
 
     # the other precision on the same inputs: FP32 PCR + FP64 refinement when the
     # headline is plain FP64 (and the reverse), for the benchmark spec's ratio
@@ -249,6 +299,8 @@ def run_ours(args, world, rank, local, pg):
         with torch.cuda.stream(stream):
             for it in range(max(3, args.steps) + 2):
                 arrs[5].copy_(rhs, non_blocking=True)
+                if small:
+                    flush.zero_()
                 ek0.record(stream)
                 osolve()
                 ek1.record(stream)
@@ -341,7 +393,9 @@ def run_ours(args, world, rank, local, pg):
         "config": {"workload": cfg["name"], "m": m, "n": n, "layout": "contiguous",
                    "solver": "pcrp_solve_f64 (bit-faithful PCR-Penta)" if args.solver == "f64"
                    else "pcrp_solve_mixed (FP32 block PCR + FP64 refinement)",
-                   "l2": "inputs larger than L2 (0.8 GB vs 129 MB), no flush",
+                   "l2": (f"inputs ({48 * m * n / 1e6:.0f} MB) smaller than twice L2: a {2 * l2 / 1e6:.0f} MB "
+                          "write between timed steps, each step timed alone") if small else
+                         f"inputs larger than L2 ({48 * m * n / 1e9:.2f} GB vs {l2 / 1e6:.0f} MB), no flush",
                    "parallelism": f"replicas x{world} (independent systems per GPU)"},
         "gpu_launches": launches,
         "opts": json.loads(args.opts) if args.opts else "autotuned defaults",
@@ -353,6 +407,8 @@ def run_ours(args, world, rank, local, pg):
                              f"({kms_med:.3f} ms); peak {peak_kind}"},
         "clocks": clk.summary(),
     }
+    if fp64_roof is not None:
+        line["fp64_roofline"] = fp64_roof
     if other is not None:
         line["compare"] = other
     if lib_cmp is not None:

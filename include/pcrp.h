@@ -224,6 +224,14 @@ int32_t pcrp_version(void);
  * a diagnostic for benchmarks.  No counterpart in the reference. */
 int64_t pcrp_kernel_launches(void);
 
+/* Measures this GPU's FP64 issue rates with two throughput kernels on
+ * `stream` (synchronous, ~a millisecond): independent DFMA chains, and
+ * independent IEEE divisions (__ddiv_rn).  Rates in operations per second.
+ * The roofline of the bit-faithful FP64 path is its FP64 instruction count
+ * over these rates; a diagnostic for benchmarks, no counterpart in the
+ * reference. */
+pcrp_status pcrp_measure_fp64(double* dfma_per_s, double* ddiv_per_s, pcrp_stream stream);
+
 /* ------------------------------------------------------------------------ */
 /* Seeded input generators (host memory, threads over systems)              */
 /* ------------------------------------------------------------------------ */

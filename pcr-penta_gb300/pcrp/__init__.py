@@ -83,6 +83,7 @@ _SIGS = {
     "pcrp_get_last_error_string": [],
     "pcrp_version": [],
     "pcrp_kernel_launches": [],
+    "pcrp_measure_fp64": [_vp, _vp, _vp],
     "pcrp_generate": [_i32, ctypes.c_uint64, _i64, _i64, _i32] + [_vp] * 6 + [_i32],
     "pcrp_generate_device": [_i32, ctypes.c_uint64, _i64, _i64, _i32] + [_vp] * 6 + [_vp],
     "pcrp_ragged_sizes": [ctypes.c_uint64, _i64, _i64, _i64, _vp],
@@ -240,6 +241,14 @@ def version() -> int:
 def kernel_launches() -> int:
     """Kernels launched by libpcrp in this process so far."""
     return int(lib().pcrp_kernel_launches())
+
+
+def measure_fp64(stream=None):
+    """(DFMA/s, IEEE FP64 divisions/s) of this GPU, from two throughput
+    kernels (pcrp_measure_fp64); synchronous."""
+    f, d = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    _check(lib().pcrp_measure_fp64(ctypes.byref(f), ctypes.byref(d), _stream(stream)), "pcrp_measure_fp64")
+    return f.value, d.value
 
 
 # ----------------------------------------------------------------------------
