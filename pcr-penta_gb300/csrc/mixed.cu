@@ -138,6 +138,54 @@ __device__ __forceinline__ double x_update(const double* __restrict__ xsrc, int6
     return x;
 }
 
+// Iterates of sweep s: x_0 in X0 when more sweeps follow, every later x_s in
+// the output; x_{s-1} is read from where sweep s-1 wrote it.
+struct XView { const double* src; int64_t sss, srs; double* dst; int64_t dss, drs; };
+
+__device__ __forceinline__ XView x_view(int s, int max_sweeps, const double* X0, double* xout, int64_t n,
+                                        int64_t oss, int64_t ors)
+{
+    XView v;
+    if (s == 0) { v.src = nullptr; v.sss = 0; v.srs = 0; }
+    else if (s == 1) { v.src = X0; v.sss = n; v.srs = 1; }
+    else { v.src = xout; v.sss = oss; v.srs = ors; }
+    if (s == 0 && max_sweeps >= 2) { v.dst = const_cast<double*>(X0); v.dss = n; v.drs = 1; }
+    else { v.dst = xout; v.dss = oss; v.drs = ors; }
+    return v;
+}
+
+// Graph-driven sweeps: the per-sweep fields from the device sweep counter
+// (written by the previous sweep's last kernel, complete before this one
+// starts).  No-ops for host-driven launches.
+__device__ __forceinline__ void mp_resolve(MpArgs& p)
+{
+    if (!p.ctr) return;
+    p.sweep = *p.ctr;
+    const XView v = x_view(p.sweep, p.max_sweeps, p.X0, p.xout, p.n, p.oss, p.ors);
+    p.xsrc = v.src; p.xsrc_ss = v.sss; p.xsrc_rs = v.srs;
+    p.xdst = v.dst; p.xdst_ss = v.dss; p.xdst_rs = v.drs;
+}
+
+__device__ __forceinline__ void mp_resolve(MpPassArgs& p)
+{
+    if (!p.ctr) return;
+    const int s = *p.ctr;
+    p.sweep = s;
+    p.live = p.live0 + s;
+    if (p.level0) p.srcY = (s & 1) ? p.R1 : p.R0;
+    if (p.pre0) {
+        unsigned* pre = p.pre0 + (size_t)s * kMpMaxPasses * p.m;
+        p.ndx_pre_in = p.pass > 0 ? pre + (size_t)(p.pass - 1) * p.m : nullptr;
+        p.ndx_pre_out = p.final_step ? nullptr : pre + (size_t)p.pass * p.m;
+    }
+    if (p.nx0) {
+        p.nx = p.nx0 + (size_t)s * p.m;
+        const XView v = x_view(s, p.max_sweeps, p.X0, p.xout, p.n, p.oss, p.ors);
+        p.xsrc = v.src; p.xsrc_ss = v.sss; p.xsrc_rs = v.srs;
+        p.xdst = v.dst; p.xdst_ss = v.dss; p.xdst_rs = v.drs;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // 2x2 helpers (row-major m[0] m[1] / m[2] m[3])
 // ---------------------------------------------------------------------------
@@ -256,7 +304,7 @@ mp_init_kernel(MpArgs p)
     for (int64_t q = t0; q < (int64_t)kMpMaxPasses * p.m; q += st) p.trunc[q] = 0u;
     for (int64_t q = t0; q < (int64_t)(p.max_sweeps + 1) * p.m; q += st) { p.ndx[q] = 0u; p.nx[q] = 0u; }
     for (int64_t q = t0; q < (int64_t)p.max_sweeps * kMpMaxPasses * p.m; q += st) p.ndx_pre[q] = 0u;
-    if (t0 == 0) *p.nfail = 0;
+    if (t0 == 0) { *p.nfail = 0; if (p.ctr) *p.ctr = 0; }
     for (int64_t q = t0; q <= p.max_sweeps; q += st) p.live[q] = (int)p.m;
 }
 
@@ -598,15 +646,17 @@ __device__ __forceinline__ void try_solve(const MpPassArgs& p, const TryTile& t,
     }
 }
 
-// Persistent CTAs over the windows, 4 per SM (40 KB tiles of 1024 rows):
-// the reduction levels are short dependent chains separated by barriers, so
-// several tiles per SM keep it busy.
-__global__ void __launch_bounds__(kMpTryThreads, 4)
+// Persistent CTAs over the windows, 5 per SM (40 KB tiles of 1024 rows, at
+// most 48 registers): the reduction levels are short dependent chains
+// separated by barriers, so several tiles per SM keep it busy.
+__global__ void __launch_bounds__(kMpTryThreads, 5)
 mp_try_kernel(MpPassArgs p)
 {
     extern __shared__ float4 fsm[];
     pdl_wait();
     pdl_release();                                // one wave of persistent CTAs: the successor may queue now
+    mp_resolve(p);
+    if (p.skip0 && p.sweep == 0) return;          // sweep 0 ran in the fused kernel
     if (__ldg(p.live) == 0) return;               // every system finished in an earlier sweep
     const int TRs = mp_pass_rows(p.TRmax);
     float4* sL = fsm;
@@ -754,6 +804,7 @@ mp_pass_kernel(MpPassArgs p)
     __shared__ unsigned s_max[1];
     pdl_wait();
     pdl_release();                                // one wave of persistent CTAs: the successor may queue now
+    mp_resolve(p);
     // the flags read here were written by earlier kernels: read-only cache
     if (__ldg(p.live) == 0) return;               // every system finished in an earlier sweep
     if (p.fail && __ldg(p.nfail) == 0) return;    // the windowed pass solved every system
@@ -801,6 +852,7 @@ mp_xupdate_kernel(MpArgs p)
     __shared__ float s_red[kMpThreads / 32];
     pdl_wait();
     pdl_release();                                // one wave of persistent CTAs: the successor may queue now
+    mp_resolve(p);
     const int s = p.sweep;
     if (__ldg(p.live + s) == 0) return;           // every system finished in an earlier sweep
     if (p.cr_mode && __ldg(p.nfail) == 0) return; // the cyclic-reduction passes updated every system
@@ -868,6 +920,7 @@ mp_decide_kernel(MpArgs p)
 {
     pdl_wait();
     pdl_release();
+    mp_resolve(p);
     const int s = p.sweep;
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     bool finish = false;
@@ -889,16 +942,16 @@ mp_decide_kernel(MpArgs p)
 // to FP32 by the power of two of the main diagonal; the odd row of a block
 // row reaches the even lane by a shuffle, which normalises the pair by the
 // block's diagonal inverse -> R[(s+1) & 1], the rhs of sweep s+1.
-__device__ __forceinline__ void residual_tile(const MpArgs& p, int64_t j, int64_t tile, double* sx)
+__device__ __forceinline__ void residual_tile(const MpArgs& p, int s, const double* __restrict__ x, int64_t xss,
+                                              int64_t xrs, int64_t j, int64_t tile, double* sx)
 {
-    const int s = p.sweep, tid = threadIdx.x;
+    const int tid = threadIdx.x;
     const int64_t n = p.n;
     constexpr int XR = kMpTile / kMpThreads;             // rows per thread
     const int64_t t0 = tile * kMpTile, t1 = min(t0 + kMpTile, n);
     const int64_t ih = tid < 2 ? t0 - 2 + tid : t1 + tid - 2;          // halo row of threads 0-3
     const bool halo = tid < 4 && ih >= 0 && ih < n;
-    const double* __restrict__ x = p.xdst;                // x_s, written by this sweep's earlier kernels
-    const int64_t xs = j * p.xdst_ss;
+    const int64_t xs = j * xss;                           // x_s, written by this sweep's earlier kernels
     double ba[XR], bb[XR], bc[XR], bd[XR], be[XR], by[XR];
 #pragma unroll
     for (int u = 0; u < XR; u++) {
@@ -908,10 +961,10 @@ __device__ __forceinline__ void residual_tile(const MpArgs& p, int64_t j, int64_
             const int64_t g = j * p.ss + i * p.rs;
             ba[u] = p.a[g]; bb[u] = p.b[g]; bc[u] = p.c[g]; bd[u] = p.d[g]; be[u] = p.e[g];
             by[u] = p.Yc[j * n + i];
-            sx[tid + u * kMpThreads + 2] = x[xs + i * p.xdst_rs];
+            sx[tid + u * kMpThreads + 2] = x[xs + i * xrs];
         }
     }
-    if (halo) sx[ih - t0 + 2] = x[xs + ih * p.xdst_rs];
+    if (halo) sx[ih - t0 + 2] = x[xs + ih * xrs];
     __syncthreads();
 
     const int64_t nb = (n + 1) / 2;
@@ -956,7 +1009,14 @@ mp_residual_kernel(MpArgs p)
     __shared__ double sx[kMpTile + 4];
     pdl_wait();
     pdl_release();                                // one wave of persistent CTAs: the successor may queue now
-    const int s = p.sweep;
+    // (resolved into locals: the argument block itself stays read-only)
+    const int s = p.ctr ? *p.ctr : p.sweep;
+    const double* x = p.xdst;
+    int64_t xss = p.xdst_ss, xrs = p.xdst_rs;
+    if (p.ctr) {
+        const XView v = x_view(s, p.max_sweeps, p.X0, p.xout, p.n, p.oss, p.ors);
+        x = v.dst; xss = v.dss; xrs = v.drs;
+    }
     if (__ldg(p.live + s + 1) == 0) return;       // every system has finished
     const bool fused0 = p.first_fused && s == 0;  // the fused sweep 0 formed r_0 of the systems it solved
     if (fused0 && __ldg(p.nfail) == 0) return;
@@ -965,9 +1025,20 @@ mp_residual_kernel(MpArgs p)
         const int64_t j = blk / tiles;
         if (__ldg(p.fin + j) != 0) continue;
         if (fused0 && !__ldg(p.fail + j)) continue;
-        residual_tile(p, j, blk - j * tiles, sx);
+        residual_tile(p, s, x, xss, xrs, j, blk - j * tiles, sx);
         __syncthreads();
     }
+}
+
+// End of a graph-driven sweep: advance the counter and tell the enclosing
+// while node whether another sweep runs (a sweep remains and a system is
+// still running).
+__global__ void mp_advance_kernel(MpArgs p, cudaGraphConditionalHandle h)
+{
+    pdl_wait();
+    const int s = *p.ctr + 1;
+    *p.ctr = s;
+    cudaGraphSetConditional(h, (s < p.max_sweeps && p.live[s] > 0) ? 1u : 0u);
 }
 
 // r = y - A x (FP64 FMA chain).  Bands and y use the caller's layout (ss, rs);
@@ -1141,6 +1212,13 @@ cudaError_t launch_mp_residual(const MpArgs& p, cudaStream_t s)
     const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
     const int64_t blocks = std::min<int64_t>(p.m * tiles, mp_grid_cap((const void*)mp_residual_kernel, kMpThreads, 0));
     const cudaError_t e = launch_dependent(mp_residual_kernel, (unsigned)blocks, kMpThreads, 0, s, p);
+    count_launch();
+    return e;
+}
+
+cudaError_t launch_mp_advance(const MpArgs& p, cudaGraphConditionalHandle h, cudaStream_t s)
+{
+    const cudaError_t e = launch_dependent(mp_advance_kernel, 1u, 1u, 0, s, p, h);
     count_launch();
     return e;
 }

@@ -1,7 +1,10 @@
 // mixed_host.cpp -- host side of the mixed-precision solver: workspace
 // layout, the FP32 pass plan and the refinement sweep loop.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "mixed_internal.h"
@@ -47,7 +50,7 @@ MpPlan mp_plan(int64_t nb, const pcrp_opts* o)
 }
 
 struct MpLayout {
-    size_t S0, R, Mi, P0, P1, dx, X0, Yc, Xout, ndx, nx, fin, status, est, trunc, ndx_pre, live, fail, nfail, rbuf, rn,
+    size_t S0, R, Mi, P0, P1, dx, X0, Yc, Xout, ctr, ndx, nx, fin, status, est, trunc, ndx_pre, live, fail, nfail, rbuf, rn,
         total;
 };
 
@@ -66,6 +69,7 @@ MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool 
     L.X0 = take((size_t)m * n * sizeof(double));
     L.Yc = take((size_t)m * n * sizeof(double));
     L.Xout = info ? take((size_t)m * n * sizeof(double)) : 0;
+    L.ctr = take(sizeof(int));
     L.ndx = take((size_t)(max_sweeps + 1) * m * sizeof(unsigned));
     L.nx = take((size_t)(max_sweeps + 1) * m * sizeof(unsigned));
     L.fin = take(m * sizeof(int));
@@ -83,6 +87,245 @@ MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool 
 }
 
 bool valid_layout(int32_t l) { return l == PCRP_LAYOUT_CONTIGUOUS || l == PCRP_LAYOUT_INTERLEAVED; }
+
+// Everything one sweep needs besides the argument block.
+struct SweepPlan {
+    MpPlan pl;
+    MpWindows W;
+    int64_t nb, T;
+    bool windowed, cr_mode, fused;
+    float* P[2];                // ping-pong state of the block-PCR passes
+};
+
+// One sweep's kernels.  s >= 0: host-driven, the per-sweep fields are set
+// here; s < 0: the body of the graph's while node, the kernels resolve them
+// on the device from the sweep counter A.ctr.
+pcrp_status enqueue_sweep(MpArgs A, const SweepPlan& S, int s, cudaStream_t st)
+{
+    const bool dev = s < 0;
+    const int64_t m = A.m, n = A.n, nb = S.nb, T = S.T;
+    const MpPlan& pl = S.pl;
+    cudaError_t ce;
+    if (!dev) {
+        A.sweep = s;
+        if (s == 0) { A.xsrc = nullptr; A.xsrc_ss = 0; A.xsrc_rs = 0; }
+        else if (s == 1) { A.xsrc = A.X0; A.xsrc_ss = n; A.xsrc_rs = 1; }
+        else { A.xsrc = A.xout; A.xsrc_ss = A.oss; A.xsrc_rs = A.ors; }
+        if (s == 0 && A.max_sweeps >= 2) { A.xdst = A.X0; A.xdst_ss = n; A.xdst_rs = 1; }
+        else { A.xdst = A.xout; A.xdst_ss = A.oss; A.xdst_rs = A.ors; }
+    }
+
+    // FP32 block solve of the normalised system with rhs R[s & 1]
+    MpPassArgs p{};
+    p.srcLU = A.S0;
+    p.dx = A.dx; p.fin = A.fin; p.ndx = A.ndx;
+    p.m = m; p.n = n; p.nb = nb; p.G = 1;
+    if (dev) {
+        p.ctr = A.ctr; p.live0 = A.live; p.R0 = A.R[0]; p.R1 = A.R[1]; p.pre0 = A.ndx_pre;
+        p.X0 = A.X0; p.xout = A.xout; p.oss = A.oss; p.ors = A.ors; p.max_sweeps = A.max_sweeps;
+    } else {
+        p.sweep = s; p.srcY = A.R[s & 1]; p.live = A.live + s;
+    }
+    unsigned* pre = dev ? nullptr : A.ndx_pre + (size_t)s * kMpMaxPasses * m;
+    if (S.cr_mode && (dev || !(S.fused && s == 0))) {
+        // cyclic reduction of whole systems or of windows that decouple
+        // within pl.win levels, with x_s = x_{s-1} + dx_s; the passes
+        // below take the systems it leaves coupled
+        MpPassArgs t = p;
+        t.K = S.W.K; t.H = S.W.H; t.L = S.W.L; t.final_step = 0; t.nwin = S.W.nwin; t.TRmax = S.W.TRmax;
+        t.fail = A.fail; t.nfail = A.nfail;
+        if (dev) {
+            t.pre0 = nullptr; t.level0 = 1; t.nx0 = A.nx; t.skip0 = S.fused;
+        } else {
+            t.xsrc = A.xsrc; t.xsrc_ss = A.xsrc_ss; t.xsrc_rs = A.xsrc_rs;
+            t.xdst = A.xdst; t.xdst_ss = A.xdst_ss; t.xdst_rs = A.xdst_rs;
+            t.nx = A.nx + (size_t)s * m;
+        }
+        ce = launch_mp_try(t, st);
+        if (ce != cudaSuccess) return cuda_error(ce, "mixed cyclic-reduction launch");
+    }
+    if (S.cr_mode) { p.fail = A.fail; p.nfail = A.nfail; }
+    int done = 0, pass = 0;
+    while (done < pl.s1) {
+        const int K = std::min(pl.fuse, pl.s1 - done);
+        const int H = (1 << K) - 1;
+        int Lw = std::max(1, pl.cap - 2 * H);
+        const int64_t nrmax = cdiv(nb, p.G);
+        char* D = reinterpret_cast<char*>(S.P[pass & 1]);
+        p.dstLU = reinterpret_cast<float4*>(D);
+        p.dstY = reinterpret_cast<float2*>(D + 2 * T * sizeof(float4));
+        p.K = K; p.H = H; p.L = Lw; p.final_step = 0;
+        p.nwin = cdiv(nrmax, Lw);
+        p.TRmax = (int)std::min<int64_t>(Lw + 2 * H, nrmax);
+        p.trunc_in = pass > 0 ? A.trunc + (pass - 1) * m : nullptr;
+        p.trunc_out = A.trunc + pass * m;
+        p.pass = pass; p.level0 = dev && pass == 0;
+        if (!dev) {
+            p.ndx_pre_in = pass > 0 ? pre + (pass - 1) * m : nullptr;
+            p.ndx_pre_out = pre + pass * m;
+        }
+        ce = launch_mp_pass(p, st);
+        if (ce != cudaSuccess) return cuda_error(ce, "mixed global pass launch");
+        p.srcLU = p.dstLU; p.srcY = p.dstY;
+        p.G <<= K; done += K; pass++;
+    }
+    if (!(S.cr_mode && pl.s1 == 0)) {            // whole systems never leave the cyclic-reduction pass
+        const int64_t nrmax = cdiv(nb, p.G);
+        int Kf = 0;
+        while ((int64_t(1) << Kf) < nrmax) Kf++;
+        p.K = Kf; p.H = 0; p.L = (int)nrmax; p.final_step = 1; p.nwin = 1; p.TRmax = (int)nrmax;
+        p.trunc_in = pass > 0 ? A.trunc + (pass - 1) * m : nullptr;
+        p.trunc_out = nullptr;
+        p.pass = pass; p.level0 = dev && pass == 0;
+        if (!dev) {
+            p.ndx_pre_in = pass > 0 ? pre + (pass - 1) * m : nullptr;
+            p.ndx_pre_out = nullptr;
+        }
+        ce = launch_mp_pass(p, st);
+        if (ce != cudaSuccess) return cuda_error(ce, "mixed shared-memory pass launch");
+        // x_s of the systems the passes solved
+        ce = launch_mp_xupdate(A, st);
+        if (ce != cudaSuccess) return cuda_error(ce, "mixed update launch");
+    }
+    // stopping decision, then the next rhs of the systems still running
+    ce = launch_mp_decide(A, st);
+    if (ce == cudaSuccess && (dev || s + 1 < A.max_sweeps)) ce = launch_mp_residual(A, st);
+    if (ce != cudaSuccess) return cuda_error(ce, "mixed refinement launch");
+    return PCRP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Graph-driven sweeps: init and sweep 0's first kernel, then a while node
+// whose body is one sweep ending in mp_advance_kernel, which stops the loop
+// once every system has finished.  Sweeps after convergence cost nothing.
+// One graph per argument set (pointers, sizes, tolerance, plan), built on
+// the second call with that set and replayed afterwards.
+// ---------------------------------------------------------------------------
+struct GraphKey {
+    int dev;
+    const void* ptr[8];
+    int64_t m, n, ss, rs;
+    double tol;
+    int max_sweeps, cap, fuse, win;
+    bool operator<(const GraphKey& o) const { return std::memcmp(this, &o, sizeof(GraphKey)) < 0; }
+};
+
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;             // kernels of the prefix and of one sweep
+    bool failed = false;         // capture or instantiation refused: host-driven from now on
+    uint64_t used = 0;
+};
+
+std::mutex g_graph_mu;
+std::map<GraphKey, GraphEntry> g_graphs;
+uint64_t g_graph_clock = 0;
+constexpr size_t kMaxGraphs = 16;
+
+bool graph_wanted(cudaStream_t st)
+{
+    if (std::getenv("PCRP_NO_GRAPH")) return false;       // host-driven sweeps only (tests of both paths)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) return false;
+    return cs == cudaStreamCaptureStatusNone;             // inside a caller's capture: plain launches
+}
+
+// Captures the graph of one solve; returns null (and clears the error) if
+// this CUDA version or device refuses any step.
+cudaGraphExec_t build_sweep_graph(const MpArgs& A, const SweepPlan& S, int* kernels)
+{
+    cudaStream_t cs = nullptr, cs2 = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const int64_t before = pcrp_kernel_launches();
+    bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+    if (ok) {
+        bool body_ok = launch_mp_init(A, cs) == cudaSuccess &&
+                       (S.fused ? launch_mp_first(A, S.W, cs) : launch_mp_prep(A, cs)) == cudaSuccess;
+        cudaStreamCaptureStatus status;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        cudaGraphConditionalHandle h = 0;
+        cudaGraphNode_t cond = nullptr;
+        cudaGraphNodeParams cp{};
+        body_ok = body_ok &&
+                  cudaStreamGetCaptureInfo(cs, &status, nullptr, &g, &deps, nullptr, &ndeps) == cudaSuccess &&
+                  cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+        if (body_ok) {
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = h;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            body_ok = cudaGraphAddNode(&cond, g, deps, nullptr, ndeps, &cp) == cudaSuccess &&
+                      cudaStreamUpdateCaptureDependencies(cs, &cond, nullptr, 1, cudaStreamSetCaptureDependencies) ==
+                          cudaSuccess;
+        }
+        if (body_ok) {
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            body_ok = cudaStreamBeginCaptureToGraph(cs2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) ==
+                      cudaSuccess;
+            if (body_ok) {
+                body_ok = enqueue_sweep(A, S, -1, cs2) == PCRP_OK && launch_mp_advance(A, h, cs2) == cudaSuccess;
+                cudaGraph_t b2 = nullptr;
+                body_ok = cudaStreamEndCapture(cs2, &b2) == cudaSuccess && body_ok;
+            }
+        }
+        const cudaError_t ee = cudaStreamEndCapture(cs, &graph);
+        ok = body_ok && ee == cudaSuccess && graph != nullptr &&
+             cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+    }
+    *kernels = (int)(pcrp_kernel_launches() - before);
+    count_launch(-*kernels);                      // counted when the graph runs, not when captured
+    if (graph) cudaGraphDestroy(graph);
+    if (cs2) cudaStreamDestroy(cs2);
+    if (cs) cudaStreamDestroy(cs);
+    if (!ok) {
+        if (exec) cudaGraphExecDestroy(exec);
+        cudaGetLastError();                       // a refused capture is not the caller's error
+        return nullptr;
+    }
+    return exec;
+}
+
+// PCRP_ENOTSUP: not (yet) graph-driven for this argument set; the caller
+// enqueues host-driven sweeps.
+pcrp_status launch_sweep_graph(const MpArgs& A, const SweepPlan& S, cudaStream_t st)
+{
+    GraphKey k;
+    std::memset(&k, 0, sizeof k);
+    if (cudaGetDevice(&k.dev) != cudaSuccess) return PCRP_ENOTSUP;
+    const void* ptrs[8] = {A.a, A.b, A.c, A.d, A.e, A.y, A.S0, A.xout};
+    for (int i = 0; i < 8; i++) k.ptr[i] = ptrs[i];
+    k.m = A.m; k.n = A.n; k.ss = A.ss; k.rs = A.rs; k.tol = A.tol; k.max_sweeps = A.max_sweeps;
+    k.cap = S.pl.cap; k.fuse = S.pl.fuse; k.win = S.pl.win;
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    auto it = g_graphs.find(k);
+    if (it == g_graphs.end()) {
+        if (g_graphs.size() >= kMaxGraphs) {      // forget the least recently used
+            auto old = g_graphs.begin();
+            for (auto jt = g_graphs.begin(); jt != g_graphs.end(); ++jt)
+                if (jt->second.used < old->second.used) old = jt;
+            if (old->second.exec) cudaGraphExecDestroy(old->second.exec);
+            g_graphs.erase(old);
+        }
+        g_graphs[k].used = ++g_graph_clock;       // first call: host-driven, remembered
+        return PCRP_ENOTSUP;
+    }
+    GraphEntry& E = it->second;
+    E.used = ++g_graph_clock;
+    if (E.failed) return PCRP_ENOTSUP;
+    if (!E.exec) {
+        E.exec = build_sweep_graph(A, S, &E.kernels);
+        if (!E.exec) { E.failed = true; return PCRP_ENOTSUP; }
+    }
+    const cudaError_t ce = cudaGraphLaunch(E.exec, st);
+    if (ce != cudaSuccess) return cuda_error(ce, "mixed sweep graph launch");
+    count_launch(E.kernels);                      // the prefix and the kernels of one sweep (the loop may repeat them)
+    return PCRP_OK;
+}
 
 }  // namespace
 
@@ -138,100 +381,49 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
 
     // Windows of the level-0 cyclic-reduction passes: whole systems when
     // they fit one tile, else windows with a 2^(win+1) halo.
-    const bool windowed = pl.s1 > 0 && pl.win > 0;
-    const bool cr_mode = pl.s1 == 0 || windowed;
-    MpWindows W{};
+    SweepPlan S{};
+    S.pl = pl; S.nb = nb; S.T = T;
+    S.windowed = pl.s1 > 0 && pl.win > 0;
+    S.cr_mode = pl.s1 == 0 || S.windowed;
     if (pl.s1 == 0) {
-        W.nwin = 1; W.L = (int)nb; W.H = 0; W.K = 31; W.TRmax = (int)nb;
-    } else if (windowed) {
-        W.H = 2 << pl.win; W.K = pl.win; W.L = kMpTryRows - 2 * W.H;
-        W.nwin = cdiv(nb, W.L);
-        W.TRmax = (int)std::min<int64_t>(W.L + 2 * W.H, nb);
+        S.W.nwin = 1; S.W.L = (int)nb; S.W.H = 0; S.W.K = 31; S.W.TRmax = (int)nb;
+    } else if (S.windowed) {
+        S.W.H = 2 << pl.win; S.W.K = pl.win; S.W.L = kMpTryRows - 2 * S.W.H;
+        S.W.nwin = cdiv(nb, S.W.L);
+        S.W.TRmax = (int)std::min<int64_t>(S.W.L + 2 * S.W.H, nb);
     }
     // Sweep 0 fused into one kernel (prep, reduction, x_0, r_0) when the
     // level-0 pass is a cyclic-reduction one and a second sweep exists.
-    const bool fused = max_sweeps >= 2 && cr_mode;
-    A.first_fused = fused;
-    A.cr_mode = cr_mode;
+    S.fused = max_sweeps >= 2 && S.cr_mode;
+    A.first_fused = S.fused;
+    A.cr_mode = S.cr_mode;
     // Iterates: x_0 in X0 when more sweeps follow, every later x_s in the
     // output (y, or Xout when y must keep the rhs for the report).
-    double* xout = keep_x ? A.Xout : y;
-    const int64_t oss = keep_x ? n : ss, ors = keep_x ? 1 : rs;
+    A.xout = keep_x ? A.Xout : y;
+    A.oss = keep_x ? n : ss;
+    A.ors = keep_x ? 1 : rs;
+    S.P[0] = pl.s1 > 0 ? F(WL.P0) : nullptr;
+    S.P[1] = pl.npass > 1 ? F(WL.P1) : nullptr;
+    A.ctr = reinterpret_cast<int*>(base + WL.ctr);
 
-    cudaError_t ce = launch_mp_init(A, st);
+    cudaError_t ce;
+    const bool graph = !keep_x && graph_wanted(st);
+    if (graph) {
+        const pcrp_status grc = launch_sweep_graph(A, S, st);
+        if (grc != PCRP_ENOTSUP) {
+            if (out) *out = A;
+            return grc;
+        }
+    }
+    // host-driven sweeps: every kernel of every sweep is enqueued here
+    A.ctr = nullptr;
+    ce = launch_mp_init(A, st);
     if (ce != cudaSuccess) return cuda_error(ce, "mixed init launch");
-    ce = fused ? launch_mp_first(A, W, st) : launch_mp_prep(A, st);
-    if (ce != cudaSuccess) return cuda_error(ce, fused ? "mixed first-sweep launch" : "mixed prep launch");
-
-    float* P[2] = {pl.s1 > 0 ? F(WL.P0) : nullptr, pl.npass > 1 ? F(WL.P1) : nullptr};
+    ce = S.fused ? launch_mp_first(A, S.W, st) : launch_mp_prep(A, st);
+    if (ce != cudaSuccess) return cuda_error(ce, S.fused ? "mixed first-sweep launch" : "mixed prep launch");
     for (int s = 0; s < max_sweeps; s++) {
-        A.sweep = s;
-        if (s == 0) { A.xsrc = nullptr; A.xsrc_ss = 0; A.xsrc_rs = 0; }
-        else if (s == 1) { A.xsrc = A.X0; A.xsrc_ss = n; A.xsrc_rs = 1; }
-        else { A.xsrc = xout; A.xsrc_ss = oss; A.xsrc_rs = ors; }
-        if (s == 0 && max_sweeps >= 2) { A.xdst = A.X0; A.xdst_ss = n; A.xdst_rs = 1; }
-        else { A.xdst = xout; A.xdst_ss = oss; A.xdst_rs = ors; }
-
-        // FP32 block solve of the normalised system with rhs R[s & 1]
-        MpPassArgs p{};
-        p.srcLU = A.S0; p.srcY = A.R[s & 1];
-        p.dx = A.dx; p.fin = A.fin; p.ndx = A.ndx; p.live = A.live + s;
-        p.m = m; p.n = n; p.nb = nb; p.G = 1; p.sweep = s;
-        unsigned* pre = A.ndx_pre + (size_t)s * kMpMaxPasses * m;
-        if (cr_mode && !(fused && s == 0)) {
-            // cyclic reduction of whole systems or of windows that decouple
-            // within pl.win levels, with x_s = x_{s-1} + dx_s; the passes
-            // below take the systems it leaves coupled
-            MpPassArgs t = p;
-            t.K = W.K; t.H = W.H; t.L = W.L; t.final_step = 0; t.nwin = W.nwin; t.TRmax = W.TRmax;
-            t.fail = A.fail; t.nfail = A.nfail;
-            t.xsrc = A.xsrc; t.xsrc_ss = A.xsrc_ss; t.xsrc_rs = A.xsrc_rs;
-            t.xdst = A.xdst; t.xdst_ss = A.xdst_ss; t.xdst_rs = A.xdst_rs;
-            t.nx = A.nx + (size_t)s * m;
-            ce = launch_mp_try(t, st);
-            if (ce != cudaSuccess) return cuda_error(ce, "mixed cyclic-reduction launch");
-        }
-        if (cr_mode) { p.fail = A.fail; p.nfail = A.nfail; }
-        int done = 0, pass = 0;
-        while (done < pl.s1) {
-            const int K = std::min(pl.fuse, pl.s1 - done);
-            const int H = (1 << K) - 1;
-            int Lw = std::max(1, pl.cap - 2 * H);
-            const int64_t nrmax = cdiv(nb, p.G);
-            char* D = reinterpret_cast<char*>(P[pass & 1]);
-            p.dstLU = reinterpret_cast<float4*>(D);
-            p.dstY = reinterpret_cast<float2*>(D + 2 * T * sizeof(float4));
-            p.K = K; p.H = H; p.L = Lw; p.final_step = 0;
-            p.nwin = cdiv(nrmax, Lw);
-            p.TRmax = (int)std::min<int64_t>(Lw + 2 * H, nrmax);
-            p.trunc_in = pass > 0 ? A.trunc + (pass - 1) * m : nullptr;
-            p.trunc_out = A.trunc + pass * m;
-            p.ndx_pre_in = pass > 0 ? pre + (pass - 1) * m : nullptr;
-            p.ndx_pre_out = pre + pass * m;
-            ce = launch_mp_pass(p, st);
-            if (ce != cudaSuccess) return cuda_error(ce, "mixed global pass launch");
-            p.srcLU = p.dstLU; p.srcY = p.dstY;
-            p.G <<= K; done += K; pass++;
-        }
-        if (!(cr_mode && pl.s1 == 0)) {            // whole systems never leave the cyclic-reduction pass
-            const int64_t nrmax = cdiv(nb, p.G);
-            int Kf = 0;
-            while ((int64_t(1) << Kf) < nrmax) Kf++;
-            p.K = Kf; p.H = 0; p.L = (int)nrmax; p.final_step = 1; p.nwin = 1; p.TRmax = (int)nrmax;
-            p.trunc_in = pass > 0 ? A.trunc + (pass - 1) * m : nullptr;
-            p.trunc_out = nullptr;
-            p.ndx_pre_in = pass > 0 ? pre + (pass - 1) * m : nullptr;
-            p.ndx_pre_out = nullptr;
-            ce = launch_mp_pass(p, st);
-            if (ce != cudaSuccess) return cuda_error(ce, "mixed shared-memory pass launch");
-            // x_s of the systems the passes solved
-            ce = launch_mp_xupdate(A, st);
-            if (ce != cudaSuccess) return cuda_error(ce, "mixed update launch");
-        }
-        // stopping decision, then the next rhs of the systems still running
-        ce = launch_mp_decide(A, st);
-        if (ce == cudaSuccess && s + 1 < max_sweeps) ce = launch_mp_residual(A, st);
-        if (ce != cudaSuccess) return cuda_error(ce, "mixed refinement launch");
+        const pcrp_status rc = enqueue_sweep(A, S, s, st);
+        if (rc != PCRP_OK) return rc;
     }
     if (out) *out = A;
     return PCRP_OK;

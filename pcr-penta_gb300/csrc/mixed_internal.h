@@ -27,6 +27,10 @@ struct MpArgs {
     int64_t xsrc_ss, xsrc_rs;           //   ... and its system / row strides
     double* xdst;                       // this sweep's x_s ...
     int64_t xdst_ss, xdst_rs;
+    double* xout;                       // the output iterate (y or Xout) and its strides: x_s of sweeps >= 1
+    int64_t oss, ors;
+    int* ctr;                           // device sweep counter (graph-driven sweeps), or null: `sweep` and the
+                                        // per-sweep fields above are set by the host for each launch
     unsigned* ndx;                      // [(max_sweeps+1) x m] max |dx| per sweep (float bits)
     unsigned* nx;                       // [(max_sweeps+1) x m] max |x| per sweep
     int* fin;                           // per system: 0 running, else the sweep it finished in, plus 1
@@ -67,6 +71,19 @@ struct MpPassArgs {
     double* xdst;                       //   ... and x_s = x_{s-1} + dx_s (null: write dx instead)
     int64_t xdst_ss, xdst_rs;
     unsigned* nx;                       //   ... and max |x_s|
+    // Graph-driven sweeps: the fields above that change from sweep to sweep
+    // (sweep, live, srcY at level 0, ndx_pre_in/out, xsrc, xdst, nx) are
+    // derived on the device from the sweep counter and these:
+    const int* ctr;                     // device sweep counter, or null (host-set fields)
+    const int* live0;
+    const float2* R0;                   // level-0 passes: rhs of even / odd sweeps
+    const float2* R1;
+    unsigned* pre0;                     // ndx_pre base
+    unsigned* nx0;                      // nx base (cyclic-reduction pass)
+    const double* X0;
+    double* xout;
+    int64_t oss, ors;
+    int pass, max_sweeps, level0, skip0;   // skip0: sweep 0 belongs to the fused kernel
     int64_t m, n, nb, G, nwin;
     int K, final_step, L, H, TRmax, sweep;
 };
@@ -107,6 +124,7 @@ cudaError_t launch_mp_try(const MpPassArgs& p, cudaStream_t s);
 cudaError_t launch_mp_xupdate(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_decide(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_residual(const MpArgs& p, cudaStream_t s);
+cudaError_t launch_mp_advance(const MpArgs& p, cudaGraphConditionalHandle h, cudaStream_t s);
 cudaError_t launch_residual(const double* a, const double* b, const double* c, const double* d, const double* e,
                             const double* y, const double* x, double* r, int64_t m, int64_t n, int64_t ss,
                             int64_t rs, int64_t xss, int64_t xrs, cudaStream_t s);

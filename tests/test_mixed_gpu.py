@@ -178,3 +178,26 @@ def test_mixed_unaligned_arrays(cuda):
     pcrp.solve_mixed(*views, m, n)
     torch.cuda.synchronize()
     assert O.fwd_err(views[5].cpu().numpy(), O.ge(*arrs, m, n), m, n) <= TOL
+
+
+@pytest.mark.parametrize("kind,m,n", [(pcrp.GEN_DOMINANT, 16, 512), (pcrp.GEN_DOMINANT, 4, 65536),
+                                      (pcrp.GEN_ADI, 8, 4096), (pcrp.GEN_ADI, 2, 20000)])
+def test_mixed_graph_driven_sweeps_match_host_driven(cuda, kind, m, n, monkeypatch):
+    """Repeated calls with one argument set run the sweeps as a CUDA graph
+    with a device-side while loop (from the second call on); the results are
+    bit-identical to the host-driven launches and every call converges."""
+    import torch
+    arrs = [torch.as_tensor(np.asarray(v)).cuda() for v in pcrp.generate(kind, 5, m, n)]
+    rhs = arrs[5].clone()
+    monkeypatch.setenv("PCRP_NO_GRAPH", "1")
+    pcrp.solve_mixed(*arrs, m, n, max_sweeps=16, report=False)
+    torch.cuda.synchronize()
+    host = arrs[5].clone()
+    monkeypatch.delenv("PCRP_NO_GRAPH")
+    for _ in range(3):
+        arrs[5].copy_(rhs)
+        pcrp.solve_mixed(*arrs, m, n, max_sweeps=16, report=False)
+        torch.cuda.synchronize()
+        assert torch.equal(arrs[5], host)
+    xg = O.ge(*[v.cpu().numpy() for v in arrs[:5]], rhs.cpu().numpy(), m, n)
+    assert O.fwd_err(host.cpu().numpy(), xg, m, n) <= (TOL if kind == pcrp.GEN_DOMINANT else 1e-11)
