@@ -141,13 +141,19 @@ pcrp_status pcrp_solve_f64_noalloc(const double* a, const double* b, const doubl
 /* Mixed precision: FP32 PCR + FP64 iterative refinement                    */
 /* ------------------------------------------------------------------------ */
 
-/* Row-scales every system by its main diagonal, solves it in FP32 with a
- * 2x2-block PCR on the CUDA cores, and refines in FP64: r = y - A x (fused
- * FP64 pentadiagonal matvec), solve for the correction in FP32, x += dx in
- * FP64, until the estimated relative forward error is <= tol or max_sweeps
- * sweeps have run (tol <= 0: 1e-12; max_sweeps <= 0: 8).  If `info` is
+/* Row-scales every system by its main diagonal, solves it in FP32 by 2x2-
+ * block reduction on the CUDA cores (cyclic reduction of whole systems or of
+ * decoupling windows, block PCR otherwise), and refines in FP64: r = y - A x
+ * (fused FP64 pentadiagonal matvec), solve for the correction in FP32,
+ * x += dx in FP64, until the estimated relative forward error is <= tol or
+ * max_sweeps sweeps have run (tol <= 0: 1e-12; max_sweeps <= 0: 8).  `a` and
+ * `e` may be NULL: that band is zero and neither read nor multiplied (NULL for
+ * both: a tridiagonal batch, a third less band traffic).  If `info` is
  * non-NULL the call synchronises `stream` and fills it; if `info` is NULL the
- * call is asynchronous and never reports PCRP_ENOCONV.
+ * call is asynchronous and never reports PCRP_ENOCONV.  From the second
+ * asynchronous call with the same arguments and workspace the sweeps run as
+ * a CUDA graph whose while node stops at convergence (environment variable
+ * PCRP_NO_GRAPH: always host-driven launches).
  * No counterpart in the reference (new work named by the solver's design). */
 pcrp_status pcrp_solve_mixed(const double* a, const double* b, const double* c,
                              const double* d, const double* e, double* y,
@@ -157,7 +163,8 @@ pcrp_status pcrp_solve_mixed(const double* a, const double* b, const double* c,
                              pcrp_mixed_info* info);
 
 /* r = y - A x in FP64 for every system (fused pentadiagonal matvec).  x, y and
- * r are device arrays of m*n doubles in `layout`; r may not alias x.
+ * r are device arrays of m*n doubles in `layout`; r may not alias x; `a` and
+ * `e` may be NULL (zero bands).
  * No counterpart in the reference. */
 pcrp_status pcrp_residual_f64(const double* a, const double* b, const double* c,
                               const double* d, const double* e, const double* y,

@@ -84,6 +84,13 @@ __device__ __forceinline__ float d2f_scaled(double v, int sh) {
     const unsigned sign = hi & 0x80000000u;
     const int E = (int)((hi >> 20) & 0x7FF);
     const int F = E - sh - (1023 - 127);                        // biased FP32 exponent of the result
+    if ((unsigned)(F - 1) < 254u && (unsigned)(E - 1) < 0x7FEu) {
+        // normal input and result (the common case): rebias the exponent in
+        // place and round the mantissa; a rounding carry into exponent 255
+        // gives inf
+        const unsigned u = ((((hi & 0x800FFFFFu) | ((unsigned)F << 20)) << 3) | (lo >> 29)) + ((lo >> 28) & 1u);
+        return __uint_as_float((u & 0x7FFFFFFFu) | sign);
+    }
     const unsigned mant = ((hi & 0xFFFFFu) << 3) | (lo >> 29);   // top 23 bits of the mantissa
     unsigned u = ((unsigned)F << 23) + mant + ((lo >> 28) & 1u);
     u = min(u, 0x7F800000u);                                     // rounded past the largest float: inf
@@ -204,7 +211,8 @@ __device__ __forceinline__ M2 minv(const M2& D) {
 
 // The six FP64 values of rows i0 = 2k and i1 = 2k+1 of one system (i1 may be
 // the dummy row n of an odd system).  Contiguous pairs at an even element
-// offset are read as one 16-byte load per array.
+// offset are read as one 16-byte load per array.  A null outer band (a or e)
+// is zero and not read.
 struct PairRow { double a0, a1, b0, b1, c0, c1, d0, d1, e0, e1, y0, y1; };
 
 __device__ __forceinline__ PairRow load_pair(const MpArgs& p, int64_t base, int64_t i0)
@@ -212,19 +220,22 @@ __device__ __forceinline__ PairRow load_pair(const MpArgs& p, int64_t base, int6
     PairRow P;
     const int64_t n = p.n, rs = p.rs;
     const int64_t g0 = base + i0 * rs;
+    const double2 z = make_double2(0.0, 0.0);
     if (p.vec && rs == 1 && ((g0 & 1) == 0) && i0 + 1 < n) {
-        const double2 a = *reinterpret_cast<const double2*>(p.a + g0);
+        const double2 a = p.a ? *reinterpret_cast<const double2*>(p.a + g0) : z;
         const double2 b = *reinterpret_cast<const double2*>(p.b + g0);
         const double2 c = *reinterpret_cast<const double2*>(p.c + g0);
         const double2 d = *reinterpret_cast<const double2*>(p.d + g0);
-        const double2 e = *reinterpret_cast<const double2*>(p.e + g0);
+        const double2 e = p.e ? *reinterpret_cast<const double2*>(p.e + g0) : z;
         const double2 y = *reinterpret_cast<const double2*>(p.y + g0);
         P = {a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x, e.y, y.x, y.y};
     } else {
-        P.a0 = p.a[g0]; P.b0 = p.b[g0]; P.c0 = p.c[g0]; P.d0 = p.d[g0]; P.e0 = p.e[g0]; P.y0 = p.y[g0];
+        P.a0 = p.a ? p.a[g0] : 0.0; P.b0 = p.b[g0]; P.c0 = p.c[g0]; P.d0 = p.d[g0];
+        P.e0 = p.e ? p.e[g0] : 0.0; P.y0 = p.y[g0];
         if (i0 + 1 < n) {
             const int64_t g1 = g0 + rs;
-            P.a1 = p.a[g1]; P.b1 = p.b[g1]; P.c1 = p.c[g1]; P.d1 = p.d[g1]; P.e1 = p.e[g1]; P.y1 = p.y[g1];
+            P.a1 = p.a ? p.a[g1] : 0.0; P.b1 = p.b[g1]; P.c1 = p.c[g1]; P.d1 = p.d[g1];
+            P.e1 = p.e ? p.e[g1] : 0.0; P.y1 = p.y[g1];
         } else {
             P.a1 = 0.0; P.b1 = 0.0; P.c1 = 1.0; P.d1 = 0.0; P.e1 = 0.0; P.y1 = 0.0;
         }
@@ -754,19 +765,19 @@ __device__ __forceinline__ void first_item(const MpArgs& p, const MpWindows& g, 
         const double2 xp = k + 1 < TR ? sX[swz(k + 1)] : make_double2(0.0, 0.0);
         double r0 = P.y0;                          // row i0: x_{i0-2..i0+2} = xm.x xm.y xc.x xc.y xp.x
         r0 = fma(-P.c0, xc.x, r0);
-        if (i0 >= 2) r0 = fma(-P.a0, xm.x, r0);
+        if (p.a && i0 >= 2) r0 = fma(-P.a0, xm.x, r0);
         if (i0 >= 1) r0 = fma(-P.b0, xm.y, r0);
         if (i0 + 1 < n) r0 = fma(-P.d0, xc.y, r0);
-        if (i0 + 2 < n) r0 = fma(-P.e0, xp.x, r0);
+        if (p.e && i0 + 2 < n) r0 = fma(-P.e0, xp.x, r0);
         float rf1 = 0.0f;                          // row i0+1 (the identity row of an odd system: 0)
         if (i0 + 1 < n) {
             const int64_t i1 = i0 + 1;             // x_{i1-2..i1+2} = xm.y xc.x xc.y xp.x xp.y
             double r1 = P.y1;
             r1 = fma(-P.c1, xc.y, r1);
-            if (i1 >= 2) r1 = fma(-P.a1, xm.y, r1);
+            if (p.a && i1 >= 2) r1 = fma(-P.a1, xm.y, r1);
             r1 = fma(-P.b1, xc.x, r1);
             if (i1 + 1 < n) r1 = fma(-P.d1, xp.x, r1);
-            if (i1 + 2 < n) r1 = fma(-P.e1, xp.y, r1);
+            if (p.e && i1 + 2 < n) r1 = fma(-P.e1, xp.y, r1);
             rf1 = d2f_scaled(r1, d_exponent(P.c1));
         }
         const float rf0 = d2f_scaled(r0, d_exponent(P.c0));
@@ -959,7 +970,8 @@ __device__ __forceinline__ void residual_tile(const MpArgs& p, int s, const doub
         ba[u] = 0.0; bb[u] = 0.0; bc[u] = 1.0; bd[u] = 0.0; be[u] = 0.0; by[u] = 0.0;
         if (i < t1) {
             const int64_t g = j * p.ss + i * p.rs;
-            ba[u] = p.a[g]; bb[u] = p.b[g]; bc[u] = p.c[g]; bd[u] = p.d[g]; be[u] = p.e[g];
+            ba[u] = p.a ? p.a[g] : 0.0; bb[u] = p.b[g]; bc[u] = p.c[g]; bd[u] = p.d[g];
+            be[u] = p.e ? p.e[g] : 0.0;
             by[u] = p.Yc[j * n + i];
             sx[tid + u * kMpThreads + 2] = x[xs + i * xrs];
         }
@@ -982,15 +994,15 @@ __device__ __forceinline__ void residual_tile(const MpArgs& p, int s, const doub
             double r = by[u];
             r = fma(-bc[u], sx[li], r);
             if (interior) {
-                r = fma(-ba[u], sx[li - 2], r);
+                if (p.a) r = fma(-ba[u], sx[li - 2], r);
                 r = fma(-bb[u], sx[li - 1], r);
                 r = fma(-bd[u], sx[li + 1], r);
-                r = fma(-be[u], sx[li + 2], r);
+                if (p.e) r = fma(-be[u], sx[li + 2], r);
             } else {
-                if (i >= 2) r = fma(-ba[u], sx[li - 2], r);
+                if (p.a && i >= 2) r = fma(-ba[u], sx[li - 2], r);
                 if (i >= 1) r = fma(-bb[u], sx[li - 1], r);
                 if (i + 1 < n) r = fma(-bd[u], sx[li + 1], r);
-                if (i + 2 < n) r = fma(-be[u], sx[li + 2], r);
+                if (p.e && i + 2 < n) r = fma(-be[u], sx[li + 2], r);
             }
             rf = d2f_scaled(r, d_exponent(bc[u]));
         }
@@ -1041,7 +1053,7 @@ __global__ void mp_advance_kernel(MpArgs p, cudaGraphConditionalHandle h)
     cudaGraphSetConditional(h, (s < p.max_sweeps && p.live[s] > 0) ? 1u : 0u);
 }
 
-// r = y - A x (FP64 FMA chain).  Bands and y use the caller's layout (ss, rs);
+// r = y - A x (FP64 FMA chain; a null outer band is zero).  Bands and y use the caller's layout (ss, rs);
 // x and r use (xss, xrs).
 __global__ void __launch_bounds__(kMpThreads)
 residual_kernel(const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
@@ -1058,10 +1070,10 @@ residual_kernel(const double* __restrict__ a, const double* __restrict__ b, cons
         const int64_t gx = j * xss + i * xrs;
         double v = y[g];
         v = fma(-c[g], x[gx], v);
-        if (i >= 2) v = fma(-a[g], x[gx - 2 * xrs], v);
+        if (a && i >= 2) v = fma(-a[g], x[gx - 2 * xrs], v);
         if (i >= 1) v = fma(-b[g], x[gx - xrs], v);
         if (i + 1 < n) v = fma(-d[g], x[gx + xrs], v);
-        if (i + 2 < n) v = fma(-e[g], x[gx + 2 * xrs], v);
+        if (e && i + 2 < n) v = fma(-e[g], x[gx + 2 * xrs], v);
         r[gx] = v;
     }
 }
@@ -1094,10 +1106,10 @@ resid_norm_kernel(const double* __restrict__ a, const double* __restrict__ b, co
     for (int64_t i = tile * 1024 + threadIdx.x; i < iend; i += blockDim.x) {
         const int64_t g = j * ss + i * rs;
         double rowsum = fabs(c[g]);
-        if (i >= 2) rowsum += fabs(a[g]);
+        if (a && i >= 2) rowsum += fabs(a[g]);
         if (i >= 1) rowsum += fabs(b[g]);
         if (i + 1 < n) rowsum += fabs(d[g]);
-        if (i + 2 < n) rowsum += fabs(e[g]);
+        if (e && i + 2 < n) rowsum += fabs(e[g]);
         rm = fmaxf(rm, (float)fabs(r[j * n + i]));
         am = fmaxf(am, (float)rowsum);
         xm = fmaxf(xm, (float)fabs(X[j * n + i]));

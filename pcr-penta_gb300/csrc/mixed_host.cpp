@@ -444,7 +444,7 @@ extern "C" pcrp_status pcrp_solve_mixed(const double* a, const double* b, const 
     if (!valid_layout(layout)) return set_error(PCRP_EINVAL, "%s: bad layout %d", who, layout);
     if (info) std::memset(info, 0, sizeof *info);
     if (m == 0 || n == 0) { if (info) info->converged = 1; return PCRP_OK; }
-    if (!a || !b || !c || !d || !e || !y) return set_error(PCRP_EINVAL, "%s: null array", who);
+    if (!b || !c || !d || !y) return set_error(PCRP_EINVAL, "%s: null array (only a and e may be null)", who);
     if (n > (int64_t(1) << 31) || m > (int64_t(1) << 24))
         return set_error(PCRP_EINVAL, "%s: size out of range (m <= 2^24, n <= 2^31)", who);
     if (!(tol > 0.0)) tol = 1e-12;
@@ -519,7 +519,8 @@ extern "C" pcrp_status pcrp_residual_f64(const double* a, const double* b, const
     if (m < 0 || n < 0) return set_error(PCRP_EINVAL, "pcrp_residual_f64: negative size");
     if (!valid_layout(layout)) return set_error(PCRP_EINVAL, "pcrp_residual_f64: bad layout %d", layout);
     if (m == 0 || n == 0) return PCRP_OK;
-    if (!a || !b || !c || !d || !e || !y || !x || !r) return set_error(PCRP_EINVAL, "pcrp_residual_f64: null array");
+    if (!b || !c || !d || !y || !x || !r)
+        return set_error(PCRP_EINVAL, "pcrp_residual_f64: null array (only a and e may be null)");
     if (r == x) return set_error(PCRP_EINVAL, "pcrp_residual_f64: r may not alias x");
     const int64_t ss = layout == PCRP_LAYOUT_CONTIGUOUS ? n : 1, rs = layout == PCRP_LAYOUT_CONTIGUOUS ? 1 : m;
     return cuda_error(launch_residual(a, b, c, d, e, y, x, r, m, n, ss, rs, ss, rs, (cudaStream_t)stream),

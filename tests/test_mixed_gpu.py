@@ -201,3 +201,34 @@ def test_mixed_graph_driven_sweeps_match_host_driven(cuda, kind, m, n, monkeypat
         assert torch.equal(arrs[5], host)
     xg = O.ge(*[v.cpu().numpy() for v in arrs[:5]], rhs.cpu().numpy(), m, n)
     assert O.fwd_err(host.cpu().numpy(), xg, m, n) <= (TOL if kind == pcrp.GEN_DOMINANT else 1e-11)
+
+
+@pytest.mark.parametrize("n", [7, 512, 5000, 65536])
+def test_mixed_tridiagonal_null_outer_bands(cuda, n):
+    """a = e = NULL: a tridiagonal batch (the outer bands are neither read nor
+    multiplied); same answers as passing zero bands, to the solver's bar."""
+    import torch
+    m = 4
+    rng = np.random.default_rng(n)
+    b, d, y = [rng.uniform(-1, 1, (m, n)) for _ in range(3)]
+    b[:, 0] = 0.0; d[:, -1] = 0.0
+    c = np.abs(b) + np.abs(d) + rng.uniform(1, 2, (m, n))
+    z = np.zeros((m, n))
+    full = [v.ravel().copy() for v in (z, b, c, d, z, y)]
+    t = [torch.as_tensor(v).cuda() for v in full]
+    info = pcrp.solve_mixed(None, t[1], t[2], t[3], None, t[5], m, n)
+    torch.cuda.synchronize()
+    x = t[5].cpu().numpy()
+    assert info.converged == 1
+    assert O.fwd_err(x, O.ge(*full, m, n), m, n) <= TOL
+    t2 = [torch.as_tensor(v).cuda() for v in full]
+    pcrp.solve_mixed(*t2, m, n, report=False)
+    torch.cuda.synchronize()
+    assert O.fwd_err(x, t2[5].cpu().numpy(), m, n) <= TOL
+
+
+def test_mixed_null_inner_band_rejected(cuda):
+    import torch
+    t = [torch.zeros(8, dtype=torch.float64, device="cuda") for _ in range(6)]
+    with pytest.raises(pcrp.PcrpError):
+        pcrp.solve_mixed(t[0], None, t[2], t[3], t[4], t[5], 1, 8)
