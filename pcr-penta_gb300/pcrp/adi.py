@@ -18,7 +18,9 @@ makes L pentadiagonal), and the theta scheme
 
 A few fully implicit start-up steps (Rannacher) damp the kink of the payoff.
 The right-hand side is formed on the device with the fused FP64 residual
-(r = 0 - (-B) u = B u) and every step calls the batched solver.  At S = 0 the
+(r = 0 - (-B) u = B u) and every step calls the batched solver; the band
+arrays of each operator are assembled once and reused by every step with the
+same (theta, dt).  At S = 0 the
 stencil needs no outside values (S_0 = 0 removes the diffusion and
 convection terms).  At S_max the values beyond the grid are extrapolated
 linearly (u_SS = 0, the far-field behaviour of a call): the ghost values
@@ -76,14 +78,30 @@ def price_call(K: torch.Tensor, v: torch.Tensor, r: float, T: float, steps: int,
     rhs = torch.empty(m * n, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream().cuda_stream
 
+    # The operators depend only on (theta, dt): assembled once per pair and
+    # reused by every step that has it (all steps after the start-up).
+    ops = {}
+
+    def operators(th: float, dtk: float):
+        key = (th, dtk)
+        if key not in ops:
+            A = operator_bands(v, n, r, -th * dtk, s_max)
+            negB = [-t for t in operator_bands(v, n, r, (1.0 - th) * dtk, s_max)] if th < 1.0 else None
+            ops[key] = (A, negB)
+        return ops[key]
+
+    # two solution buffers used in turn: every other step repeats the solver's
+    # arguments, so its sweeps run as a replayed graph
+    bufs = [torch.empty(m * n, dtype=torch.float64, device=dev) for _ in range(2)]
+
     def step(th: float, dtk: float, u_flat: torch.Tensor) -> torch.Tensor:
-        A = operator_bands(v, n, r, -th * dtk, s_max)
-        if th < 1.0:
-            negB = [-t for t in operator_bands(v, n, r, (1.0 - th) * dtk, s_max)]
+        A, negB = operators(th, dtk)
+        x = bufs[1] if u_flat.data_ptr() == bufs[0].data_ptr() else bufs[0]
+        if negB is not None:
             residual_f64(*negB, zero, u_flat, rhs, m, n, CONTIGUOUS, stream=stream)   # rhs = B u
-            x = rhs.clone()
+            x.copy_(rhs)
         else:
-            x = u_flat.clone()
+            x.copy_(u_flat)
         if solver == "mixed":
             solve_mixed(*A, x, m, n, CONTIGUOUS, tol=tol, stream=stream, report=False)
         else:
