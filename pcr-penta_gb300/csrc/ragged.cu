@@ -219,7 +219,7 @@ cudaError_t enqueue(const RgArgs& a, int grid, cudaStream_t s)
     const int pg = (int)std::min<int64_t>(std::max<int64_t>(1, cdiv64(a.nsys, 256)), 1024);
     rg_plan_kernel<<<pg, 256, 0, s>>>(a);
     rg_scan_kernel<<<1, 1024, 0, s>>>(a);
-    const size_t smem = (size_t)a.cap * 14 * sizeof(double);
+    const size_t smem = (size_t)a.cap * kSmemArrays * sizeof(double);
     rg_persistent_kernel<<<grid, kRgThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
@@ -301,8 +301,8 @@ pcrp_status ragged_f64(const double* a, const double* b, const double* c, const 
     int dev = 0;
     ce = cudaGetDevice(&dev);
     if (ce != cudaSuccess) return cuda_error(ce, "cudaGetDevice");
-    const size_t smem = (size_t)cap * 14 * sizeof(double);
-    ce = cudaFuncSetAttribute(rg_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kRgCap * 14 * sizeof(double)));
+    const size_t smem = (size_t)cap * kSmemArrays * sizeof(double);
+    ce = cudaFuncSetAttribute(rg_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kRgCap * kSmemArrays * sizeof(double)));
     if (ce != cudaSuccess) return cuda_error(ce, "cudaFuncSetAttribute");
     int per_sm = 0, sms = 0;
     ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rg_persistent_kernel, kRgThreads, smem);
