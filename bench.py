@@ -139,8 +139,9 @@ def dist_setup(args):
     return world, rank, local, pg
 
 
-def cpu_sample_gunk(cfg, systems: int, reps: int = 1):
-    """Oracle PCR restatement on `systems` systems of the workload, all cores."""
+def cpu_sample_gunk(cfg, systems: int, reps: int = 1, solver: str = "pcr"):
+    """Oracle PCR restatement (or, solver="ge", the FP64 banded Gaussian
+    elimination) on `systems` systems of the workload, all cores."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     import pcrp
@@ -151,7 +152,10 @@ def cpu_sample_gunk(cfg, systems: int, reps: int = 1):
     best = None
     for _ in range(reps):
         t = time.perf_counter()
-        O.pcr(*arrs, m, n, threads=cores)
+        if solver == "ge":
+            O.ge(*arrs, m, n, threads=cores)
+        else:
+            O.pcr(*arrs, m, n, threads=cores)
         dt = time.perf_counter() - t
         best = dt if best is None else min(best, dt)
     return m * n / best / 1e9, cores, best
@@ -434,6 +438,12 @@ def run_ours(args, world, rank, local, pg):
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"{min(m, args.ref_systems)} of {m} systems (n={n}), "
                                           f"oracle PCR restatement, {dt:.2f} s wall"}
+        # the FP64 host solver the accuracy is judged against: banded
+        # Gaussian elimination, threads over systems (a reported baseline)
+        gv, gcores, gdt = cpu_sample_gunk(cfg, min(m, args.ref_systems), reps=2, solver="ge")
+        line["host_ge"] = {"value": gv, "unit": UNIT, "cores": gcores,
+                           "sample": f"{min(m, args.ref_systems)} of {m} systems (n={n}), FP64 banded "
+                                     f"Gaussian elimination (oracle), {gdt:.3f} s wall"}
     print(json.dumps(line), flush=True)
 
 
