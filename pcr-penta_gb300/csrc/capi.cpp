@@ -187,8 +187,11 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
         if (L + 2 * H > pcr_max_smem_rows()) L = pcr_max_smem_rows() - 2 * H;
         if (L < 1) return set_error(PCRP_EINVAL, "%s: fuse_strides=%d leaves no tile rows", who, K);
         const int64_t nrmax = ceil_div(n, p.G);
-        p.K = K; p.H = H; p.L = L; p.final_step = 0;
+        // windows of equal length (at most L): no nearly empty last window per
+        // subsystem (results do not depend on where windows start)
         p.nwin = ceil_div(nrmax, L);
+        L = (int)ceil_div(nrmax, p.nwin);
+        p.K = K; p.H = H; p.L = L; p.final_step = 0;
         p.TRmax = (int)std::min<int64_t>(L + 2 * H, nrmax);
         for (int k = 0; k < NSTATE; k++) p.dst[k] = bufs[cur][k];
         p.dst_ss = n; p.dst_rs = 1;
