@@ -222,57 +222,68 @@ std::map<GraphKey, GraphEntry> g_graphs;
 uint64_t g_graph_clock = 0;
 constexpr size_t kMaxGraphs = 16;
 
-bool graph_wanted(cudaStream_t st)
+// 0: host-driven sweeps; 1: replayed graph; 2: the caller is capturing `st`:
+// the device-side loop goes into the caller's graph
+int graph_mode(cudaStream_t st)
 {
-    if (std::getenv("PCRP_NO_GRAPH")) return false;       // host-driven sweeps only (tests of both paths)
+    if (std::getenv("PCRP_NO_GRAPH")) return 0;           // host-driven sweeps only (tests of both paths)
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) return false;
-    return cs == cudaStreamCaptureStatusNone;             // inside a caller's capture: plain launches
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) return 0;
+    if (cs == cudaStreamCaptureStatusActive) return 2;
+    return cs == cudaStreamCaptureStatusNone ? 1 : 0;
+}
+
+// Appends one solve to the capture in progress on `st`: init and sweep 0's
+// first kernel, then a while node whose body (captured on a helper stream)
+// is one sweep ending in mp_advance_kernel.  Returns false if this CUDA
+// version or device refuses a step (the capture is then unusable).
+bool capture_sweep_loop(const MpArgs& A, const SweepPlan& S, cudaStream_t st)
+{
+    if (launch_mp_init(A, st) != cudaSuccess) return false;
+    if ((S.fused ? launch_mp_first(A, S.W, st) : launch_mp_prep(A, st)) != cudaSuccess) return false;
+    cudaStreamCaptureStatus status;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cudaGraphConditionalHandle h = 0;
+    if (cudaStreamGetCaptureInfo(st, &status, nullptr, &g, &deps, nullptr, &ndeps) != cudaSuccess ||
+        status != cudaStreamCaptureStatusActive ||
+        cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess)
+        return false;
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cond = nullptr;
+    if (cudaGraphAddNode(&cond, g, deps, nullptr, ndeps, &cp) != cudaSuccess ||
+        cudaStreamUpdateCaptureDependencies(st, &cond, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
+        return false;
+    cudaStream_t bs = nullptr;
+    if (cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking) != cudaSuccess) return false;
+    bool ok = cudaStreamBeginCaptureToGraph(bs, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeRelaxed) == cudaSuccess;
+    if (ok) {
+        ok = enqueue_sweep(A, S, -1, bs) == PCRP_OK && launch_mp_advance(A, h, bs) == cudaSuccess;
+        cudaGraph_t body = nullptr;
+        ok = cudaStreamEndCapture(bs, &body) == cudaSuccess && ok;
+    }
+    cudaStreamDestroy(bs);
+    return ok;
 }
 
 // Captures the graph of one solve; returns null (and clears the error) if
 // this CUDA version or device refuses any step.
 cudaGraphExec_t build_sweep_graph(const MpArgs& A, const SweepPlan& S, int* kernels)
 {
-    cudaStream_t cs = nullptr, cs2 = nullptr;
+    cudaStream_t cs = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     const int64_t before = pcrp_kernel_launches();
     bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed) == cudaSuccess;
     if (ok) {
-        bool body_ok = launch_mp_init(A, cs) == cudaSuccess &&
-                       (S.fused ? launch_mp_first(A, S.W, cs) : launch_mp_prep(A, cs)) == cudaSuccess;
-        cudaStreamCaptureStatus status;
-        cudaGraph_t g = nullptr;
-        const cudaGraphNode_t* deps = nullptr;
-        size_t ndeps = 0;
-        cudaGraphConditionalHandle h = 0;
-        cudaGraphNode_t cond = nullptr;
-        cudaGraphNodeParams cp{};
-        body_ok = body_ok &&
-                  cudaStreamGetCaptureInfo(cs, &status, nullptr, &g, &deps, nullptr, &ndeps) == cudaSuccess &&
-                  cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
-        if (body_ok) {
-            cp.type = cudaGraphNodeTypeConditional;
-            cp.conditional.handle = h;
-            cp.conditional.type = cudaGraphCondTypeWhile;
-            cp.conditional.size = 1;
-            body_ok = cudaGraphAddNode(&cond, g, deps, nullptr, ndeps, &cp) == cudaSuccess &&
-                      cudaStreamUpdateCaptureDependencies(cs, &cond, nullptr, 1, cudaStreamSetCaptureDependencies) ==
-                          cudaSuccess;
-        }
-        if (body_ok) {
-            cudaGraph_t body = cp.conditional.phGraph_out[0];
-            body_ok = cudaStreamBeginCaptureToGraph(cs2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) ==
-                      cudaSuccess;
-            if (body_ok) {
-                body_ok = enqueue_sweep(A, S, -1, cs2) == PCRP_OK && launch_mp_advance(A, h, cs2) == cudaSuccess;
-                cudaGraph_t b2 = nullptr;
-                body_ok = cudaStreamEndCapture(cs2, &b2) == cudaSuccess && body_ok;
-            }
-        }
+        const bool body_ok = capture_sweep_loop(A, S, cs);
         const cudaError_t ee = cudaStreamEndCapture(cs, &graph);
         ok = body_ok && ee == cudaSuccess && graph != nullptr &&
              cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
@@ -280,7 +291,6 @@ cudaGraphExec_t build_sweep_graph(const MpArgs& A, const SweepPlan& S, int* kern
     *kernels = (int)(pcrp_kernel_launches() - before);
     count_launch(-*kernels);                      // counted when the graph runs, not when captured
     if (graph) cudaGraphDestroy(graph);
-    if (cs2) cudaStreamDestroy(cs2);
     if (cs) cudaStreamDestroy(cs);
     if (!ok) {
         if (exec) cudaGraphExecDestroy(exec);
@@ -407,13 +417,18 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     A.ctr = reinterpret_cast<int*>(base + WL.ctr);
 
     cudaError_t ce;
-    const bool graph = !keep_x && graph_wanted(st);
-    if (graph) {
+    const int gm = keep_x ? 0 : graph_mode(st);
+    if (gm == 1) {
         const pcrp_status grc = launch_sweep_graph(A, S, st);
         if (grc != PCRP_ENOTSUP) {
             if (out) *out = A;
             return grc;
         }
+    } else if (gm == 2) {
+        if (!capture_sweep_loop(A, S, st))
+            return set_error(PCRP_ECUDA, "pcrp_solve_mixed: the sweep loop could not be added to the stream's capture");
+        if (out) *out = A;
+        return PCRP_OK;
     }
     // host-driven sweeps: every kernel of every sweep is enqueued here
     A.ctr = nullptr;

@@ -5,9 +5,11 @@
 // identity rows with zero right-hand side, and the couplings that would reach
 // them -- the out-of-range slots d_{n-1}, e_{n-2}, e_{n-1} -- are zeroed), so
 // the padded solution restricted to the first n rows is the system's own.
-// Each class runs the uniform mixed-precision solver (FP32 block PCR + FP64
-// refinement), then the solutions are scattered back.  The whole sequence is
-// captured once into a CUDA graph per (pointers, sizes) and replayed.
+// Each class runs the uniform mixed-precision solver (FP32 block reduction +
+// FP64 refinement, its sweep loop a while node that stops at convergence),
+// then the solutions are scattered back.  The classes are independent
+// branches of one CUDA graph, captured once per (pointers, sizes) and
+// replayed.
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -126,23 +128,27 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
         while (N < n) N <<= 1;
         cls[N].push_back(k);
     }
-    // workspace: [system lists | counter | padded batch | mixed scratch]
-    size_t pad = 0, mix = 0;
+    // workspace: [system lists | counter | per class: padded batch, mixed scratch]
+    // (every class has its own, so that the classes run concurrently)
+    auto r256 = [](size_t v) { return (v + 255) / 256 * 256; };
+    std::vector<size_t> pad_off, mix_off;
+    size_t per_class = 0;
     for (auto& kv : cls) {
         const int64_t ms = (int64_t)kv.second.size(), N = kv.first;
-        pad = std::max(pad, (size_t)6 * ms * N * sizeof(double));
-        mix = std::max(mix, mixed_workspace_bytes(ms, N, o, max_sweeps, false));
+        pad_off.push_back(per_class);
+        per_class += r256((size_t)6 * ms * N * sizeof(double));
+        mix_off.push_back(per_class);
+        per_class += r256(mixed_workspace_bytes(ms, N, o, max_sweeps, false));
     }
-    const size_t lists = ((size_t)nsys * sizeof(int64_t) + 255) / 256 * 256;
-    const size_t total = lists + 256 + (pad + 255) / 256 * 256 + mix;
+    const size_t lists = r256((size_t)nsys * sizeof(int64_t));
+    const size_t total = lists + 256 + per_class;
     void* ws = nullptr;
     pcrp_status rc = get_workspace(o, total, st, &ws);
     if (rc != PCRP_OK) return rc;
     char* base = static_cast<char*>(ws);
     int64_t* d_lists = reinterpret_cast<int64_t*>(base);
     int* d_unconv = reinterpret_cast<int*>(base + lists);
-    double* d_pad = reinterpret_cast<double*>(base + lists + 256);
-    void* d_mix = base + lists + 256 + (pad + 255) / 256 * 256;
+    char* d_class = base + lists + 256;
 
     std::vector<int64_t> h_lists;
     h_lists.reserve(nsys);
@@ -172,31 +178,48 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
         if (it != g_exec.end()) { exec = it->second.first; kernels = it->second.second; }
     }
     if (!exec) {
+        // One graph: the counter reset, then every size class on its own
+        // branch (gather, mixed solve with its device-side sweep loop,
+        // scatter), joined at the end.
+        const size_t ncls = cls.size();
         cudaStream_t cst = nullptr;
+        std::vector<cudaStream_t> bst(ncls, nullptr);
+        std::vector<cudaEvent_t> bev(ncls + 1, nullptr);
         ce = cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking);
-        if (ce != cudaSuccess) return cuda_error(ce, "cudaStreamCreate");
+        for (size_t q = 0; q < ncls && ce == cudaSuccess; q++) ce = cudaStreamCreateWithFlags(&bst[q], cudaStreamNonBlocking);
+        for (size_t q = 0; q <= ncls && ce == cudaSuccess; q++) ce = cudaEventCreateWithFlags(&bev[q], cudaEventDisableTiming);
         cudaGraph_t g = nullptr;
         pcrp_status prc = PCRP_OK;
         const int64_t before = pcrp_kernel_launches();
-        ce = cudaStreamBeginCapture(cst, cudaStreamCaptureModeThreadLocal);
+        if (ce == cudaSuccess) ce = cudaStreamBeginCapture(cst, cudaStreamCaptureModeRelaxed);
         if (ce == cudaSuccess) {
             cudaError_t le = cudaMemsetAsync(d_unconv, 0, sizeof(int), cst);
+            if (le == cudaSuccess) le = cudaEventRecord(bev[ncls], cst);
             int64_t at = 0;
+            size_t q = 0;
             for (auto& kv : cls) {
                 if (le != cudaSuccess || prc != PCRP_OK) break;
                 const int64_t ms = (int64_t)kv.second.size(), N = kv.first;
                 const int64_t* sys = d_lists + at;
                 at += ms;
-                rgm_gather_kernel<<<grid_for(ms * N), 256, 0, cst>>>(a, b, c, d, e, y, offsets, sys, ms, N, d_pad);
+                cudaStream_t cs = bst[q];
+                double* d_pad = reinterpret_cast<double*>(d_class + pad_off[q]);
+                void* d_mix = d_class + mix_off[q];
+                le = cudaStreamWaitEvent(cs, bev[ncls], 0);
+                if (le != cudaSuccess) break;
+                rgm_gather_kernel<<<grid_for(ms * N), 256, 0, cs>>>(a, b, c, d, e, y, offsets, sys, ms, N, d_pad);
                 count_launch();
                 const int64_t T = ms * N;
                 MpArgs A{};
                 prc = mixed_enqueue(d_pad, d_pad + T, d_pad + 2 * T, d_pad + 3 * T, d_pad + 4 * T, d_pad + 5 * T,
-                                    ms, N, N, 1, tol, max_sweeps, o, false, d_mix, cst, &A);
+                                    ms, N, N, 1, tol, max_sweeps, o, false, d_mix, cs, &A);
                 if (prc != PCRP_OK) break;
-                rgm_scatter_kernel<<<grid_for(T), 256, 0, cst>>>(d_pad + 5 * T, offsets, sys, ms, N, y, A.status, d_unconv);
+                rgm_scatter_kernel<<<grid_for(T), 256, 0, cs>>>(d_pad + 5 * T, offsets, sys, ms, N, y, A.status, d_unconv);
                 count_launch();
                 le = cudaGetLastError();
+                if (le == cudaSuccess) le = cudaEventRecord(bev[q], cs);
+                if (le == cudaSuccess) le = cudaStreamWaitEvent(cst, bev[q], 0);
+                q++;
             }
             cudaError_t ee = cudaStreamEndCapture(cst, &g);
             if (ce == cudaSuccess) ce = le != cudaSuccess ? le : ee;
@@ -205,7 +228,9 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
         count_launch(-kernels);              // counted when the graph runs, not when captured
         if (ce == cudaSuccess && prc == PCRP_OK) ce = cudaGraphInstantiate(&exec, g, 0);
         if (g) cudaGraphDestroy(g);
-        cudaStreamDestroy(cst);
+        for (auto ev : bev) if (ev) cudaEventDestroy(ev);
+        for (auto bs : bst) if (bs) cudaStreamDestroy(bs);
+        if (cst) cudaStreamDestroy(cst);
         if (prc != PCRP_OK) return prc;
         if (ce != cudaSuccess) return cuda_error(ce, "ragged mixed graph capture");
         std::lock_guard<std::mutex> lk(g_mu);

@@ -232,3 +232,30 @@ def test_mixed_null_inner_band_rejected(cuda):
     t = [torch.zeros(8, dtype=torch.float64, device="cuda") for _ in range(6)]
     with pytest.raises(pcrp.PcrpError):
         pcrp.solve_mixed(t[0], None, t[2], t[3], t[4], t[5], 1, 8)
+
+
+@pytest.mark.parametrize("mode", ["global", "thread_local", "relaxed"])
+def test_mixed_inside_a_caller_graph_capture(cuda, mode):
+    """Inside a caller's stream capture the solve (sweep loop included, as a
+    while node) becomes part of the caller's graph; replaying that graph
+    solves whatever the captured buffers hold, to the solver's bar."""
+    import torch
+    m, n = 8, 20000
+    src = [torch.as_tensor(np.asarray(v)).cuda() for v in pcrp.generate(pcrp.GEN_DOMINANT, 9, m, n)]
+    arrs = [v.clone() for v in src]
+    ws = torch.empty(pcrp.workspace_size(m, n, which=1), dtype=torch.uint8, device="cuda")
+    opts = pcrp.Opts(workspace=ws.data_ptr(), workspace_bytes=ws.numel())
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s, capture_error_mode=mode):
+            pcrp.solve_mixed(*arrs, m, n, opts=opts, stream=s, report=False)
+    for seed in (9, 10):
+        fresh = [torch.as_tensor(np.asarray(v)).cuda() for v in pcrp.generate(pcrp.GEN_DOMINANT, seed, m, n)]
+        for dst, v in zip(arrs, fresh):
+            dst.copy_(v)
+        g.replay()
+        torch.cuda.synchronize()
+        host = [v.cpu().numpy() for v in fresh]
+        assert O.fwd_err(arrs[5].cpu().numpy(), O.ge(*host, m, n), m, n) <= TOL
