@@ -34,6 +34,18 @@
 // part, so this kernel is bounded by the FP64 pipe, not HBM; the design goal
 // is to keep that pipe busy (several CTAs per SM, 4 rows per thread for ILP)
 // and to spend no FP64 operation beyond the reference's own arithmetic.
+//
+// Zero operands.  Operations whose result IEEE 754 fixes without rounding
+// (a product with a zero factor: the zero of the factors' sign xor; a sum
+// with a zero term: the other term, or -0 only if both are -0; a zero
+// numerator over a finite nonzero divisor) are formed on the integer pipe,
+// an FP64 operation costing ~40 integer operations of pipe time here and a
+// division with a zero numerator ~2.6 normal ones.  They matter once the
+// outer coefficients a, e of a diagonally dominant system have underflowed
+// to zero (from stride ~2^8-2^10 on): a vote per stride tells whether every
+// row of the tile is in that state (a = e = 0, the rest finite); then phase
+// A forms no FP64 value and phase B only its quotients and the products and
+// sums whose operands are nonzero.  Same bits as the FP64 operations.
 #include "pcr_tile.cuh"
 
 namespace pcrp {

@@ -10,13 +10,45 @@ namespace pcrp {
 __device__ __forceinline__ double mul(double x, double y) { return __dmul_rn(x, y); }
 __device__ __forceinline__ double add(double x, double y) { return __dadd_rn(x, y); }
 __device__ __forceinline__ double sub(double x, double y) { return __dsub_rn(x, y); }
-__device__ __forceinline__ double dvd(double x, double y) { return __ddiv_rn(x, y); }
+// x / y, IEEE round-to-nearest.  A zero x over a nonzero finite y is the
+// signed zero IEEE 754 prescribes (sign of x xor sign of y), formed on the
+// integer pipe: the FP64 division takes ~2.6x its normal time for a zero
+// numerator, and from stride ~2^9 on the outer coefficients of a diagonally
+// dominant system are zero, so half of the divisions of the late strides
+// have one.  Every other operand pair goes to the division.
+__device__ __forceinline__ double dvd(double x, double y) {
+    const long long xb = __double_as_longlong(x), yb = __double_as_longlong(y);
+    const long long kExp = 0x7FF0000000000000LL;
+    if ((xb << 1) == 0 && (yb << 1) != 0 && (yb & kExp) != kExp)
+        return __longlong_as_double((xb ^ yb) & (long long)0x8000000000000000ULL);
+    return __ddiv_rn(x, y);
+}
 // x != 0.0 evaluated on the integer pipe (same truth table: false for +-0,
 // true for everything else including NaN), sparing the FP64 pipe a compare
 __device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) << 1) != 0; }
 // -x by flipping the sign bit on the integer pipe (bit-identical to unary minus)
 __device__ __forceinline__ double neg(double x) {
     return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+}
+
+// Exact IEEE results of operations with a zero operand, formed on the
+// integer pipe (an FP64 operation costs ~40 integer operations of pipe time
+// here), for the strides after the outer coefficients have decayed to zero.
+__device__ __forceinline__ unsigned hiw(double x) { return (unsigned)__double2hiint(x); }
+// the zero whose sign is bit 31 of s
+__device__ __forceinline__ double szero(unsigned s) { return __hiloint2double((int)(s & 0x80000000u), 0); }
+// x + z for a zero z with sign bit zs, x not NaN: x itself, unless x is a
+// zero too (then -0 only if both are -0: round-to-nearest)
+__device__ __forceinline__ double add_z(double x, unsigned zs) { return nz(x) ? x : szero(hiw(x) & zs); }
+__device__ __forceinline__ bool finite4(double p, double q, double r, double s) {
+    return max(max(hiw(p) & 0x7FF00000u, hiw(q) & 0x7FF00000u), max(hiw(r) & 0x7FF00000u, hiw(s) & 0x7FF00000u))
+           < 0x7FF00000u;
+}
+// "zero state" of a row: outer coefficients a, e zero, the others finite.
+// While every row a stride reads is in it, both multipliers of phase A are
+// zeros, every product with them is a zero and phase A forms no FP64 value.
+__device__ __forceinline__ bool zero_state(double a, double b, double c, double d, double e, double y) {
+    return !nz(a) && !nz(e) && finite4(b, c, d, y);
 }
 
 constexpr int kMaxThreads = 256;
@@ -66,21 +98,27 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
     const double* __restrict__ gy = p.src[Y_] + soff;
 
     double al1p[RPT], al2p[RPT];
+    bool zrow = true;           // every row this thread holds in the zero state
 #pragma unroll
     for (int q = 0; q < RPT; q++) {
         const int k = tid + q * bd;
         al1p[q] = 0.0; al2p[q] = 0.0;
         if (k < TR) {
             const int64_t gi = (t0 + k) * sstep;
-            sa[k] = gload<kL2Only>(ga + gi); sb[k] = gload<kL2Only>(gb + gi); sc[k] = gload<kL2Only>(gc + gi);
-            sd[k] = gload<kL2Only>(gd + gi); se[k] = gload<kL2Only>(ge + gi); sy[k] = gload<kL2Only>(gy + gi);
+            const double a = gload<kL2Only>(ga + gi), b = gload<kL2Only>(gb + gi), c = gload<kL2Only>(gc + gi);
+            const double d = gload<kL2Only>(gd + gi), e = gload<kL2Only>(ge + gi), y = gload<kL2Only>(gy + gi);
+            sa[k] = a; sb[k] = b; sc[k] = c; sd[k] = d; se[k] = e; sy[k] = y;
+            zrow = zrow && zero_state(a, b, c, d, e, y);
             if (p.src[AL1_]) {
                 al1p[q] = gload<kL2Only>(p.src[AL1_] + soff + gi);
                 al2p[q] = gload<kL2Only>(p.src[AL2_] + soff + gi);
             }
         }
     }
-    __syncthreads();
+    // rows read by a stride are the rows the previous stride wrote (all
+    // loaded rows for the first): one vote per stride tells whether the
+    // whole tile is in the zero state
+    int ztile = __syncthreads_and(zrow);
 
     for (int s = 0; s < p.K; s++) {
         const int dl = 1 << s;
@@ -95,6 +133,58 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
         const int64_t Tlo = max(rlo - dl, (int64_t)0), Thi = min(rhi + dl, nr);
 
         // ---- phase A: T(m) = a1*row(m-d) + row(m) + a2*row(m+d) ----------
+        if (ztile) {
+            // a1 = -a(m)/b(m-d) and a2 = -e(m)/d(m+d) are zeros (b, d finite):
+            // only their signs are formed; every product with them is the
+            // zero of sign xor, every sum row m's value (kernel.cu:63-117)
+#pragma unroll
+            for (int q = 0; q < RPT; q++) {
+                const int k = tid + q * bd;
+                const int64_t t = t0 + k;
+                if (k < TR && t >= Tlo && t < Thi) {
+                    const bool hasL = t - dl >= 0, hasR = t + dl <= nr - 1;
+                    if (hasL || hasR) {
+                        const double bm = sb[k], cm = sc[k], dm = sd[k], ym = sy[k];
+                        unsigned s1 = 0u, s2 = 0u;
+                        if (hasL && t - 2 * dl >= 0) {
+                            const double bL = sb[k - dl];
+                            if (nz(bL)) s1 = (hiw(sa[k]) ^ hiw(bL)) ^ 0x80000000u;
+                        }
+                        if (hasR && t + 2 * dl <= nr - 1) {
+                            const double dR = sd[k + dl];
+                            if (nz(dR)) s2 = (hiw(se[k]) ^ hiw(dR)) ^ 0x80000000u;
+                        }
+                        // sign bits of the products a1*row(m-d) and a2*row(m+d)
+                        // (+0 for a missing neighbour: adding +0 keeps -0 out)
+                        unsigned La = 0u, Lc = 0u, Ld = 0u, Le = 0u, Ly = 0u;
+                        unsigned Ra = 0u, Rb = 0u, Rc = 0u, Re = 0u, Ry = 0u;
+                        if (hasL) {
+                            La = s1 ^ hiw(sa[k - dl]); Lc = s1 ^ hiw(sc[k - dl]); Ld = s1 ^ hiw(sd[k - dl]);
+                            Le = s1 ^ hiw(se[k - dl]); Ly = s1 ^ hiw(sy[k - dl]);
+                        }
+                        if (hasR) {
+                            Ra = s2 ^ hiw(sa[k + dl]); Rb = s2 ^ hiw(sb[k + dl]); Rc = s2 ^ hiw(sc[k + dl]);
+                            Re = s2 ^ hiw(se[k + dl]); Ry = s2 ^ hiw(sy[k + dl]);
+                        }
+                        if (hasL && hasR) {
+                            Ta[k] = szero(La);
+                            Tb[k] = add_z(bm, Lc & Ra); Tc[k] = add_z(cm, Ld & Rb);
+                            Td[k] = add_z(dm, Le & Rc); Te[k] = szero(Re);
+                            Tk[k] = add_z(ym, Ly & Ry);
+                        } else if (hasR) {     // kernel.cu:82-91: aT = bT = 0
+                            Ta[k] = 0.0; Tb[k] = 0.0;
+                            Tc[k] = add_z(cm, Rb); Td[k] = add_z(dm, Rc); Te[k] = szero(Re);
+                            Tk[k] = add_z(ym, Ry);
+                        } else {               // kernel.cu:108-117: dT = eT = 0
+                            Ta[k] = szero(La); Tb[k] = add_z(bm, Lc); Tc[k] = add_z(cm, Ld);
+                            Td[k] = 0.0; Te[k] = 0.0;
+                            Tk[k] = add_z(ym, Ly);
+                        }
+                        T1[k] = szero(s1); T2[k] = szero(s2);
+                    }
+                }
+            }
+        } else {
 #pragma unroll
         for (int q = 0; q < RPT; q++) {
             const int k = tid + q * bd;
@@ -144,44 +234,94 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                 }
             }
         }
+        }
         __syncthreads();
 
         // ---- phase B: new row = b/cT(i-d)*T(i-d) - row(i) + d/cT(i+d)*T(i+d)
+        zrow = true;
+        // the reference's update of row i (kernel.cu:120-140, in place: phase
+        // B reads no other row's state); folds the row's zero state into zrow
+        auto row_b = [&](int q, int k, bool hasL, bool hasR, double a1pre, double a2pre) {
+            const double ai = sa[k], bi = sb[k], ci = sc[k], di = sd[k], ei = se[k], yi = sy[k];
+            double a1 = 0.0, b1 = 0.0, c1 = 0.0, d1 = 0.0, k1 = 0.0, f1 = a1pre;
+            double b2 = 0.0, c2 = 0.0, d2 = 0.0, e2 = 0.0, k2 = 0.0, f2 = a2pre;
+            if (hasL) {                    // kernel.cu:120-125
+                const double cTL = Tc[k - dl];
+                if (nz(cTL)) f1 = dvd(bi, cTL);
+                a1 = mul(f1, Ta[k - dl]); b1 = mul(f1, Tb[k - dl]); c1 = mul(f1, Td[k - dl]);
+                d1 = mul(f1, Te[k - dl]); k1 = mul(f1, Tk[k - dl]);
+            }
+            if (hasR) {                    // kernel.cu:127-132
+                const double cTR = Tc[k + dl];
+                if (nz(cTR)) f2 = dvd(di, cTR);
+                c2 = mul(f2, Tb[k + dl]); b2 = mul(f2, Ta[k + dl]); d2 = mul(f2, Td[k + dl]);
+                e2 = mul(f2, Te[k + dl]); k2 = mul(f2, Tk[k + dl]);
+            }
+            const double nb = add(sub(b1, ai), b2), nc = add(sub(c1, ci), c2);   // kernel.cu:138-140
+            const double nd = add(sub(d1, ei), d2), ny = add(sub(k1, yi), k2);
+            sb[k] = nb; sc[k] = nc; sd[k] = nd; sy[k] = ny;
+            sa[k] = a1; se[k] = e2;
+            al1p[q] = f1; al2p[q] = f2;
+            zrow = zrow && zero_state(a1, nb, nc, nd, e2, ny);
+        };
+        if (ztile) {
+            // zero state: aT, eT of both neighbours and a, e of row i are
+            // zeros, so are a1, d1, b2, e2 (for finite f1, f2), and the b and
+            // d sums reduce to one term
 #pragma unroll
-        for (int q = 0; q < RPT; q++) {
-            const int k = tid + q * bd;
-            const int64_t t = t0 + k;
-            if (k < TR && t >= rlo && t < rhi) {
-                const bool hasL = t - dl >= 0, hasR = t + dl <= nr - 1;
-                const double ai = sa[k], bi = sb[k], ci = sc[k], di = sd[k], ei = se[k], yi = sy[k];
-                // multipliers last assigned before Reduction-III (kernel.cu:96-112)
-                const double a1pre = hasR ? T1[k + dl] : ((t - 2 * dl >= 0) ? T1[k - dl] : al1p[q]);
-                const double a2pre = (t + 2 * dl <= nr - 1) ? T2[k + dl] : (hasL ? T2[k - dl] : al2p[q]);
-                double a1 = 0.0, b1 = 0.0, c1 = 0.0, d1 = 0.0, k1 = 0.0, f1 = a1pre;
-                double b2 = 0.0, c2 = 0.0, d2 = 0.0, e2 = 0.0, k2 = 0.0, f2 = a2pre;
-                if (hasL) {                // kernel.cu:120-125
-                    const double cTL = Tc[k - dl];
-                    if (nz(cTL)) f1 = dvd(bi, cTL);
-                    a1 = mul(f1, Ta[k - dl]); b1 = mul(f1, Tb[k - dl]); c1 = mul(f1, Td[k - dl]);
-                    d1 = mul(f1, Te[k - dl]); k1 = mul(f1, Tk[k - dl]);
+            for (int q = 0; q < RPT; q++) {
+                const int k = tid + q * bd;
+                const int64_t t = t0 + k;
+                if (k < TR && t >= rlo && t < rhi) {
+                    const bool hasL = t - dl >= 0, hasR = t + dl <= nr - 1;
+                    // multipliers last assigned before Reduction-III (kernel.cu:96-112)
+                    const double a1pre = hasR ? T1[k + dl] : ((t - 2 * dl >= 0) ? T1[k - dl] : al1p[q]);
+                    const double a2pre = (t + 2 * dl <= nr - 1) ? T2[k + dl] : (hasL ? T2[k - dl] : al2p[q]);
+                    double f1 = a1pre, f2 = a2pre;
+                    if (hasL) { const double cTL = Tc[k - dl]; if (nz(cTL)) f1 = dvd(sb[k], cTL); }
+                    if (hasR) { const double cTR = Tc[k + dl]; if (nz(cTR)) f2 = dvd(sd[k], cTR); }
+                    if (finite4(hasL ? f1 : 0.0, hasR ? f2 : 0.0, 0.0, 0.0)) {
+                        const double ai = sa[k], ci = sc[k], ei = se[k], yi = sy[k];
+                        const unsigned s1 = hiw(f1), s2 = hiw(f2);
+                        unsigned a1s = 0u, d1s = 0u, b2s = 0u, e2s = 0u;
+                        double b1 = 0.0, c1 = 0.0, k1 = 0.0, c2 = 0.0, d2 = 0.0, k2 = 0.0;
+                        if (hasL) {
+                            a1s = s1 ^ hiw(Ta[k - dl]); d1s = s1 ^ hiw(Te[k - dl]);
+                            b1 = mul(f1, Tb[k - dl]); c1 = mul(f1, Td[k - dl]); k1 = mul(f1, Tk[k - dl]);
+                        }
+                        if (hasR) {
+                            b2s = s2 ^ hiw(Ta[k + dl]); e2s = s2 ^ hiw(Te[k + dl]);
+                            c2 = mul(f2, Tb[k + dl]); d2 = mul(f2, Td[k + dl]); k2 = mul(f2, Tk[k + dl]);
+                        }
+                        // b1 - ai + b2 with ai, b2 zeros; d1 - ei + d2 with d1, ei zeros
+                        const double nb = add_z(add_z(b1, hiw(ai) ^ 0x80000000u), b2s);
+                        const double nc = add(sub(c1, ci), c2);
+                        const double nd = add_z(d2, d1s & (hiw(ei) ^ 0x80000000u));
+                        const double ny = add(sub(k1, yi), k2);
+                        sb[k] = nb; sc[k] = nc; sd[k] = nd; sy[k] = ny;
+                        sa[k] = szero(a1s); se[k] = szero(e2s);
+                        al1p[q] = f1; al2p[q] = f2;
+                        zrow = zrow && finite4(nb, nc, nd, ny);
+                    } else {
+                        row_b(q, k, hasL, hasR, a1pre, a2pre);
+                    }
                 }
-                if (hasR) {                // kernel.cu:127-132
-                    const double cTR = Tc[k + dl];
-                    if (nz(cTR)) f2 = dvd(di, cTR);
-                    c2 = mul(f2, Tb[k + dl]); b2 = mul(f2, Ta[k + dl]); d2 = mul(f2, Td[k + dl]);
-                    e2 = mul(f2, Te[k + dl]); k2 = mul(f2, Tk[k + dl]);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < RPT; q++) {
+                const int k = tid + q * bd;
+                const int64_t t = t0 + k;
+                if (k < TR && t >= rlo && t < rhi) {
+                    const bool hasL = t - dl >= 0, hasR = t + dl <= nr - 1;
+                    // multipliers last assigned before Reduction-III (kernel.cu:96-112)
+                    const double a1pre = hasR ? T1[k + dl] : ((t - 2 * dl >= 0) ? T1[k - dl] : al1p[q]);
+                    const double a2pre = (t + 2 * dl <= nr - 1) ? T2[k + dl] : (hasL ? T2[k - dl] : al2p[q]);
+                    row_b(q, k, hasL, hasR, a1pre, a2pre);
                 }
-                // kernel.cu:138-140 (in place: phase B reads no other row's state)
-                sb[k] = add(sub(b1, ai), b2);
-                sc[k] = add(sub(c1, ci), c2);
-                sd[k] = add(sub(d1, ei), d2);
-                sy[k] = add(sub(k1, yi), k2);
-                sa[k] = a1;
-                se[k] = e2;
-                al1p[q] = f1; al2p[q] = f2;
             }
         }
-        __syncthreads();
+        ztile = __syncthreads_and(zrow);
     }
 
     if (p.final_step) {

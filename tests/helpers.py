@@ -18,6 +18,32 @@ def dd_bands(rng, m, n, garbage=False):
     return [v.ravel().copy() for v in (a, b, c, d, e, y)]
 
 
+def zero_bands(rng, m, n, special=False):
+    """Batch whose outer bands a, e are zeros of random sign (a pentadiagonal
+    system already in the state of the late strides, where every product of
+    the multipliers has a zero factor), with zeros of random sign sprinkled
+    into b, d and y; `special` adds +-inf and NaN entries to a few systems."""
+    def signed_zeros(shape):
+        return np.where(rng.random(shape) < 0.5, 0.0, -0.0)
+    a, e = signed_zeros((m, n)), signed_zeros((m, n))
+    b, d, y = [rng.uniform(-1, 1, (m, n)) for _ in range(3)]
+    for arr in (b, d, y):
+        hit = rng.random((m, n)) < 0.05
+        arr[hit] = signed_zeros(int(hit.sum()))
+    c = np.abs(b) + np.abs(d) + rng.uniform(1, 2, (m, n))
+    a[:, :2] = 0.0; b[:, :1] = 0.0; d[:, n - 1:] = 0.0; e[:, max(n - 2, 0):] = 0.0
+    if special and m >= 4 and n >= 8:
+        c[1, n // 2] = np.inf
+        y[2, n // 3] = np.nan
+        b[3, n // 4] = -np.inf
+        d[0, n // 5] = np.inf
+    # one system keeps nonzero outer bands only in its first half, so the
+    # rows of one tile mix both kinds
+    a[m - 1, 2:n // 2] = rng.uniform(-0.1, 0.1, n // 2 - 2)
+    e[m - 1, :n // 2] = rng.uniform(-0.1, 0.1, n // 2)
+    return [v.ravel().copy() for v in (a, b, c, d, e, y)]
+
+
 def to_layout(arrs, m, n, layout):
     if layout == pcrp.CONTIGUOUS:
         return [np.ascontiguousarray(v) for v in arrs]
@@ -38,8 +64,9 @@ def gpu_f64(arrs, m, n, layout=pcrp.CONTIGUOUS, path="auto", opts=None, dev="cud
 
 
 def assert_bitexact(x, xref, what=""):
-    x = np.asarray(x); xref = np.asarray(xref)
-    same = (x == xref) | (np.isnan(x) & np.isnan(xref))
+    """Equal bit patterns (so +0 and -0 differ); any NaN matches any NaN."""
+    x = np.ascontiguousarray(x, dtype=np.float64); xref = np.ascontiguousarray(xref, dtype=np.float64)
+    same = (x.view(np.uint64) == xref.view(np.uint64)) | (np.isnan(x) & np.isnan(xref))
     if not same.all():
         bad = np.flatnonzero(~same)
         k = bad[0]

@@ -11,7 +11,7 @@ import pytest
 
 import oracle as O
 import pcrp
-from helpers import assert_bitexact, dd_bands, gpu_f64, to_device, to_layout
+from helpers import assert_bitexact, dd_bands, gpu_f64, to_device, to_layout, zero_bands
 
 pytestmark = pytest.mark.gpu
 
@@ -86,6 +86,26 @@ def test_adi_and_toeplitz_bitexact(cuda):
         arrs = pcrp.generate(kind, 5, m, n)
         x, _ = gpu_f64(arrs, m, n)
         assert_bitexact(x, O.pcr(*arrs, m, n), f"kind={kind} n={n}")
+
+
+@pytest.mark.parametrize("n,path,opts", [
+    (64, "small", None), (1000, "small", None), (1024, "small", None),
+    (4096, "split", None), (5001, "split", pcrp.Opts(smem_rows=256, fuse_strides=3, tile_rows=100)),
+    (65536, "auto", None)])
+@pytest.mark.parametrize("special", [False, True])
+def test_zero_outer_bands_bitexact(cuda, n, path, opts, special):
+    """Zero outer bands (signed zeros), zeros in b, d, y, and +-inf / NaN
+    entries: the rows whose products have zero factors are formed on the
+    integer pipe and must give the bits of the IEEE operations, zero signs
+    included; rows with a non-finite operand take the FP64 operations."""
+    rng = np.random.default_rng(n + 7 * special)
+    m = 6
+    arrs = zero_bands(rng, m, n, special=special)
+    x, _ = gpu_f64(arrs, m, n, path=path, opts=opts)
+    ref = O.pcr(*arrs, m, n)
+    if not special:
+        assert np.isfinite(ref).all()
+    assert_bitexact(x, ref, f"zero bands n={n} path={path} special={special}")
 
 
 def test_bands_are_not_modified(cuda):
