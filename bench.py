@@ -47,14 +47,36 @@ def ref_strides(n: int) -> int:
 
 
 def fp64_ops(n: int):
-    """FP64 operations per unknown of the faithful solve (the reference's
-    arithmetic, division pairs shared as in the kernels): per row and stride 4
-    IEEE divisions and 36 rounded products or sums; then x = y/c for powers of
-    two, or the 2x2 pairs (per row: 1 division, 3 products/sums)."""
+    """FP64 operations per unknown of the reference's arithmetic on n rows
+    (kernel.cu:63-153, the two neighbour combinations shared as T(m)),
+    counted row by row with the boundary rows' shorter forms and nonzero
+    pivots: phase A 18 products/sums and up to 2 IEEE divisions per interior
+    row (7 and up to 1 with one neighbour), phase B 8 sums plus 5 products and
+    1 division per neighbour; then x = y/c (powers of two) or the 2x2 pairs
+    (9 products/sums and 2 divisions per pair, 1 division per single row)."""
+    import numpy as np
     s = ref_strides(n)
-    if n >= 2 and (1 << s) == n:
-        return 36 * s, 4 * s + 1
-    return 36 * s + 3, 4 * s + 1
+    t = np.arange(n, dtype=np.int64)
+    ops = divs = 0
+    for k in range(s):
+        dl = 1 << k
+        hasL, hasR = t - dl >= 0, t + dl <= n - 1
+        inner, onlyR, onlyL = hasL & hasR, hasR & ~hasL, hasL & ~hasR
+        divL, divR = t - 2 * dl >= 0, t + 2 * dl <= n - 1
+        ops += 18 * int(inner.sum()) + 7 * int((onlyR | onlyL).sum())
+        divs += int((inner & divL).sum()) + int((inner & divR).sum())
+        divs += int((onlyR & divR).sum()) + int((onlyL & divL).sum())
+        ops += 8 * n + 5 * int(hasL.sum()) + 5 * int(hasR.sum())
+        divs += int(hasL.sum()) + int(hasR.sum())
+    if n >= 1 and (1 << s) == n:
+        divs += n
+    else:
+        df = 1 << s
+        pairs = max(n - df, 0)
+        ops += 9 * pairs
+        divs += 2 * pairs + max(min(df, n) - pairs, 0)
+    return ops / n, divs / n
+
 
 CONFIGS = {
     "c0": dict(m=1024, n=512, kind=0, name="plain FP64 PCR, shared-memory path, m=1024 n=512"),
@@ -286,11 +308,16 @@ def run_ours(args, world, rank, local, pg):
         dfma, ddiv = pcrp.measure_fp64(stream)
         ops, divs = fp64_ops(n)
         t_peak = m * n * (ops / dfma + divs / ddiv)
-        fp64_roof = {"bound": "fp64", "ops_per_unknown": ops, "divisions_per_unknown": divs,
+        fp64_roof = {"bound": "fp64", "ops": "reference", "ops_per_unknown": round(ops, 2),
+                     "divisions_per_unknown": round(divs, 3),
                      "dfma_per_s": dfma, "ddiv_per_s": ddiv,
                      "ms_at_peak": t_peak * 1e3, "frac": t_peak / (kms_med * 1e-3),
-                     "note": "FP64 products/sums at the measured DFMA rate plus IEEE divisions at the "
-                             "measured division rate (pcrp_measure_fp64), over the solve's kernel time"}
+                     "note": "the reference's FP64 products/sums (exact count on n rows) at the measured "
+                             "DFMA rate plus its IEEE divisions at the measured division rate "
+                             "(pcrp_measure_fp64), over the solve's kernel time; the kernels form "
+                             "operations with a zero operand (late strides, once a and e have "
+                             "underflowed) on the integer pipe, so frac is the rate of the reference's "
+                             "operations, not the FP64 pipe's busy share (ncu reports that)"}
 
     # the other precision on the same inputs: FP32 PCR + FP64 refinement when the
     # headline is plain FP64 (and the reverse), for the benchmark spec's ratio

@@ -42,8 +42,10 @@
 // an FP64 operation costing ~40 integer operations of pipe time here and a
 // division with a zero numerator ~2.6 normal ones.  They matter once the
 // outer coefficients a, e of a diagonally dominant system have underflowed
-// to zero (from stride ~2^8-2^10 on): a vote per stride tells whether every
-// row of the tile is in that state (a = e = 0, the rest finite); then phase
+// to zero (from stride ~2^8-2^10 on): in passes whose longest stride is at
+// least 1024 rows a vote per stride tells whether every row of the tile is in
+// that state (a = e = 0, the rest finite; passes of shorter strides are
+// compiled without the vote and its cost); then phase
 // A forms no FP64 value and phase B only its quotients and the products and
 // sums whose operands are nonzero.  Same bits as the FP64 operations.
 #include "pcr_tile.cuh"
@@ -51,7 +53,7 @@
 namespace pcrp {
 namespace {
 
-template <int RPT>
+template <int RPT, bool kZero>
 __global__ void __launch_bounds__(kMaxThreads, 2)
 pcr_pass_kernel(const PcrPassArgs p)
 {
@@ -61,20 +63,33 @@ pcr_pass_kernel(const PcrPassArgs p)
     const int64_t w    = blk - item * p.nwin;
     const int64_t j    = item / p.G;
     const int64_t r    = item - j * p.G;
-    pcr_tile<RPT>(p, j, r, w, smem);
+    pcr_tile<RPT, false, kZero>(p, j, r, w, smem);
 }
 
+
+template <int RPT, bool kZero>
+cudaError_t launch_rz(const PcrPassArgs& p, int threads, size_t smem, int64_t blocks, cudaStream_t s)
+{
+    // per-device attribute; cheap, and legal while a stream is being captured
+    cudaError_t e = cudaFuncSetAttribute(pcr_pass_kernel<RPT, kZero>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         pcr_max_smem_rows() * kSmemArrays * (int)sizeof(double));
+    if (e != cudaSuccess) return e;
+    pcr_pass_kernel<RPT, kZero><<<(unsigned)blocks, threads, smem, s>>>(p);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// Passes whose longest stride reaches kZeroStride rows vote on the zero
+// state: the outer coefficients of diagonally dominant systems underflow at
+// strides ~2^8-2^10, and the vote (~10% of a dense stride) pays once two or
+// more strides of the pass run in that state.  Others keep the plain kernel.
+constexpr int64_t kZeroStride = 1024;
 
 template <int RPT>
 cudaError_t launch_rpt(const PcrPassArgs& p, int threads, size_t smem, int64_t blocks, cudaStream_t s)
 {
-    // per-device attribute; cheap, and legal while a stream is being captured
-    cudaError_t e = cudaFuncSetAttribute(pcr_pass_kernel<RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         pcr_max_smem_rows() * kSmemArrays * (int)sizeof(double));
-    if (e != cudaSuccess) return e;
-    pcr_pass_kernel<RPT><<<(unsigned)blocks, threads, smem, s>>>(p);
-    count_launch();
-    return cudaGetLastError();
+    if (p.K > 0 && (p.G << (p.K - 1)) >= kZeroStride) return launch_rz<RPT, true>(p, threads, smem, blocks, s);
+    return launch_rz<RPT, false>(p, threads, smem, blocks, s);
 }
 
 }  // namespace

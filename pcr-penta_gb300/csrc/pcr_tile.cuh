@@ -64,7 +64,10 @@ __device__ __forceinline__ double gload(const double* p) {
 
 // One CTA's work: window w of subsystem r of system j (whole subsystem when
 // p.final_step).  Every thread of the CTA must call it with the same (j, r, w).
-template <int RPT, bool kL2Only = false>
+// kZero compiles the zero-state vote and its integer-pipe strides in; without
+// it every stride takes the FP64 operations (passes of short strides, where
+// the outer coefficients have not underflowed yet, skip the vote's cost).
+template <int RPT, bool kL2Only = false, bool kZero = true>
 __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_t r, int64_t w, double* smem)
 {
     const int TRm = p.TRmax;
@@ -108,7 +111,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
             const double a = gload<kL2Only>(ga + gi), b = gload<kL2Only>(gb + gi), c = gload<kL2Only>(gc + gi);
             const double d = gload<kL2Only>(gd + gi), e = gload<kL2Only>(ge + gi), y = gload<kL2Only>(gy + gi);
             sa[k] = a; sb[k] = b; sc[k] = c; sd[k] = d; se[k] = e; sy[k] = y;
-            zrow = zrow && zero_state(a, b, c, d, e, y);
+            if constexpr (kZero) zrow = zrow && zero_state(a, b, c, d, e, y);
             if (p.src[AL1_]) {
                 al1p[q] = gload<kL2Only>(p.src[AL1_] + soff + gi);
                 al2p[q] = gload<kL2Only>(p.src[AL2_] + soff + gi);
@@ -118,7 +121,9 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
     // rows read by a stride are the rows the previous stride wrote (all
     // loaded rows for the first): one vote per stride tells whether the
     // whole tile is in the zero state
-    int ztile = __syncthreads_and(zrow);
+    int ztile = 0;
+    if constexpr (kZero) ztile = __syncthreads_and(zrow);
+    else __syncthreads();
 
     for (int s = 0; s < p.K; s++) {
         const int dl = 1 << s;
@@ -133,7 +138,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
         const int64_t Tlo = max(rlo - dl, (int64_t)0), Thi = min(rhi + dl, nr);
 
         // ---- phase A: T(m) = a1*row(m-d) + row(m) + a2*row(m+d) ----------
-        if (ztile) {
+        if (kZero && ztile) {
             // a1 = -a(m)/b(m-d) and a2 = -e(m)/d(m+d) are zeros (b, d finite):
             // only their signs are formed; every product with them is the
             // zero of sign xor, every sum row m's value (kernel.cu:63-117)
@@ -262,9 +267,9 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
             sb[k] = nb; sc[k] = nc; sd[k] = nd; sy[k] = ny;
             sa[k] = a1; se[k] = e2;
             al1p[q] = f1; al2p[q] = f2;
-            zrow = zrow && zero_state(a1, nb, nc, nd, e2, ny);
+            if constexpr (kZero) zrow = zrow && zero_state(a1, nb, nc, nd, e2, ny);
         };
-        if (ztile) {
+        if (kZero && ztile) {
             // zero state: aT, eT of both neighbours and a, e of row i are
             // zeros, so are a1, d1, b2, e2 (for finite f1, f2), and the b and
             // d sums reduce to one term
@@ -321,7 +326,8 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                 }
             }
         }
-        ztile = __syncthreads_and(zrow);
+        if constexpr (kZero) ztile = __syncthreads_and(zrow);
+        else __syncthreads();
     }
 
     if (p.final_step) {

@@ -91,6 +91,8 @@ def test_adi_and_toeplitz_bitexact(cuda):
 @pytest.mark.parametrize("n,path,opts", [
     (64, "small", None), (1000, "small", None), (1024, "small", None),
     (4096, "split", None), (5001, "split", pcrp.Opts(smem_rows=256, fuse_strides=3, tile_rows=100)),
+    (1000, "auto", pcrp.Opts(smem_rows=16, fuse_strides=6, tile_rows=50)),
+    (300, "auto", pcrp.Opts(smem_rows=8, fuse_strides=3, tile_rows=7)),
     (65536, "auto", None)])
 @pytest.mark.parametrize("special", [False, True])
 def test_zero_outer_bands_bitexact(cuda, n, path, opts, special):
