@@ -10,6 +10,18 @@ namespace pcrp {
 __device__ __forceinline__ double mul(double x, double y) { return __dmul_rn(x, y); }
 __device__ __forceinline__ double add(double x, double y) { return __dadd_rn(x, y); }
 __device__ __forceinline__ double sub(double x, double y) { return __dsub_rn(x, y); }
+// Bits of x other than the sign, OR-folded into one word: zero exactly for
+// +-0.  Written in PTX on the two 32-bit halves so that it stays on the
+// integer pipe (the equivalent C bit test can be turned into an FP64 compare,
+// which here takes a slot of the FP64 pipe).
+__device__ __forceinline__ unsigned magbits(double x) {
+    unsigned r;
+    asm("{\n\t.reg .b32 lo, hi;\n\tmov.b64 {lo, hi}, %1;\n\tshl.b32 hi, hi, 1;\n\tor.b32 %0, hi, lo;\n\t}"
+        : "=r"(r) : "d"(x));
+    return r;
+}
+// x != 0.0 (false for +-0, true for everything else including NaN)
+__device__ __forceinline__ bool nz(double x) { return magbits(x) != 0u; }
 // x / y, IEEE round-to-nearest.  A zero x over a nonzero finite y is the
 // signed zero IEEE 754 prescribes (sign of x xor sign of y), formed on the
 // integer pipe: the FP64 division takes ~2.6x its normal time for a zero
@@ -17,18 +29,18 @@ __device__ __forceinline__ double sub(double x, double y) { return __dsub_rn(x, 
 // dominant system are zero, so half of the divisions of the late strides
 // have one.  Every other operand pair goes to the division.
 __device__ __forceinline__ double dvd(double x, double y) {
-    const long long xb = __double_as_longlong(x), yb = __double_as_longlong(y);
-    const long long kExp = 0x7FF0000000000000LL;
-    if ((xb << 1) == 0 && (yb << 1) != 0 && (yb & kExp) != kExp)
-        return __longlong_as_double((xb ^ yb) & (long long)0x8000000000000000ULL);
+    const unsigned yh = (unsigned)__double2hiint(y);
+    if (magbits(x) == 0u && magbits(y) != 0u && (yh & 0x7FF00000u) != 0x7FF00000u)
+        return __hiloint2double((int)((((unsigned)__double2hiint(x)) ^ yh) & 0x80000000u), 0);
     return __ddiv_rn(x, y);
 }
-// x != 0.0 evaluated on the integer pipe (same truth table: false for +-0,
-// true for everything else including NaN), sparing the FP64 pipe a compare
-__device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) << 1) != 0; }
-// -x by flipping the sign bit on the integer pipe (bit-identical to unary minus)
+// -x by flipping the sign bit on the integer pipe (bit-identical to unary
+// minus), in PTX for the same reason as magbits
 __device__ __forceinline__ double neg(double x) {
-    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+    double r;
+    asm("{\n\t.reg .b32 lo, hi;\n\tmov.b64 {lo, hi}, %1;\n\txor.b32 hi, hi, 0x80000000;\n\tmov.b64 %0, {lo, hi};\n\t}"
+        : "=d"(r) : "d"(x));
+    return r;
 }
 
 // Exact IEEE results of operations with a zero operand, formed on the
