@@ -114,6 +114,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
 
     double al1p[RPT], al2p[RPT];
     bool zrow = true;           // every row this thread holds in the zero state
+    bool zdrow = true;          // ... with d = 0 as well
 #pragma unroll
     for (int q = 0; q < RPT; q++) {
         const int k = tid + q * bd;
@@ -123,7 +124,10 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
             const double a = gload<kL2Only>(ga + gi), b = gload<kL2Only>(gb + gi), c = gload<kL2Only>(gc + gi);
             const double d = gload<kL2Only>(gd + gi), e = gload<kL2Only>(ge + gi), y = gload<kL2Only>(gy + gi);
             sa[k] = a; sb[k] = b; sc[k] = c; sd[k] = d; se[k] = e; sy[k] = y;
-            if constexpr (kZero) zrow = zrow && zero_state(a, b, c, d, e, y);
+            if constexpr (kZero) {
+                const bool z = zero_state(a, b, c, d, e, y);
+                zrow = zrow && z; zdrow = zdrow && z && !nz(d);
+            }
             if (p.src[AL1_]) {
                 al1p[q] = gload<kL2Only>(p.src[AL1_] + soff + gi);
                 al2p[q] = gload<kL2Only>(p.src[AL2_] + soff + gi);
@@ -131,10 +135,10 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
         }
     }
     // rows read by a stride are the rows the previous stride wrote (all
-    // loaded rows for the first): one vote per stride tells whether the
-    // whole tile is in the zero state
-    int ztile = 0;
-    if constexpr (kZero) ztile = __syncthreads_and(zrow);
+    // loaded rows for the first): votes per stride tell whether the whole
+    // tile is in the zero state, and in it with d = 0 too
+    int ztile = 0, zdtile = 0;
+    if constexpr (kZero) { ztile = __syncthreads_and(zrow); zdtile = __syncthreads_and(zdrow); }
     else __syncthreads();
 
     for (int s = 0; s < p.K; s++) {
@@ -255,7 +259,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
         __syncthreads();
 
         // ---- phase B: new row = b/cT(i-d)*T(i-d) - row(i) + d/cT(i+d)*T(i+d)
-        zrow = true;
+        zrow = true; zdrow = true;
         // the reference's update of row i (kernel.cu:120-140, in place: phase
         // B reads no other row's state); folds the row's zero state into zrow
         auto row_b = [&](int q, int k, bool hasL, bool hasR, double a1pre, double a2pre) {
@@ -279,9 +283,59 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
             sb[k] = nb; sc[k] = nc; sd[k] = nd; sy[k] = ny;
             sa[k] = a1; se[k] = e2;
             al1p[q] = f1; al2p[q] = f2;
-            if constexpr (kZero) zrow = zrow && zero_state(a1, nb, nc, nd, e2, ny);
+            if constexpr (kZero) {
+                const bool z = zero_state(a1, nb, nc, nd, e2, ny);
+                zrow = zrow && z; zdrow = zdrow && z && !nz(nd);
+            }
         };
-        if (kZero && ztile) {
+        if (kZero && zdtile) {
+            // zero state with d = 0: f2 = d(i)/cT(i+d) is a zero, and so is
+            // every product with it; dT of the neighbours is zero, so c1 is
+            // too: besides the quotient f1 only b1, k1 and k1 - y(i) are FP64
+#pragma unroll
+            for (int q = 0; q < RPT; q++) {
+                const int k = tid + q * bd;
+                const int64_t t = t0 + k;
+                if (k < TR && t >= rlo && t < rhi) {
+                    const bool hasL = t - dl >= 0, hasR = t + dl <= nr - 1;
+                    // multipliers last assigned before Reduction-III (kernel.cu:96-112)
+                    const double a1pre = hasR ? T1[k + dl] : ((t - 2 * dl >= 0) ? T1[k - dl] : al1p[q]);
+                    const double a2pre = (t + 2 * dl <= nr - 1) ? T2[k + dl] : (hasL ? T2[k - dl] : al2p[q]);
+                    double f1 = a1pre, f2 = a2pre;
+                    if (hasL) { const double cTL = Tc[k - dl]; if (nz(cTL)) f1 = dvd(sb[k], cTL); }
+                    if (hasR) { const double cTR = Tc[k + dl]; if (nz(cTR)) f2 = dvd(sd[k], cTR); }
+                    // f2 is the stored multiplier where cT(i+d) = 0: then the row
+                    // takes the reference's operations
+                    if (finite4(hasL ? f1 : 0.0, 0.0, 0.0, 0.0) && (!hasR || !nz(f2))) {
+                        const double ai = sa[k], ci = sc[k], ei = se[k], yi = sy[k];
+                        const unsigned s1 = hiw(f1), s2 = hiw(f2);
+                        unsigned a1s = 0u, c1s = 0u, d1s = 0u, b2s = 0u, c2s = 0u, d2s = 0u, e2s = 0u, k2s = 0u;
+                        double b1 = 0.0, k1 = 0.0;
+                        if (hasL) {
+                            a1s = s1 ^ hiw(Ta[k - dl]); c1s = s1 ^ hiw(Td[k - dl]); d1s = s1 ^ hiw(Te[k - dl]);
+                            b1 = mul(f1, Tb[k - dl]); k1 = mul(f1, Tk[k - dl]);
+                        }
+                        if (hasR) {
+                            b2s = s2 ^ hiw(Ta[k + dl]); c2s = s2 ^ hiw(Tb[k + dl]); d2s = s2 ^ hiw(Td[k + dl]);
+                            e2s = s2 ^ hiw(Te[k + dl]); k2s = s2 ^ hiw(Tk[k + dl]);
+                        }
+                        // (b1 - ai) + b2, (c1 - ci) + c2, (d1 - ei) + d2, (k1 - yi) + k2
+                        // with zeros ai, b2, c1, c2, d1, ei, d2, k2
+                        const double nb = add_z(add_z(b1, hiw(ai) ^ 0x80000000u), b2s);
+                        const double nc = add_z(add_z(neg(ci), c1s), c2s);
+                        const double nd = szero(d1s & (hiw(ei) ^ 0x80000000u) & d2s);
+                        const double ny = add_z(sub(k1, yi), k2s);
+                        sb[k] = nb; sc[k] = nc; sd[k] = nd; sy[k] = ny;
+                        sa[k] = szero(a1s); se[k] = szero(e2s);
+                        al1p[q] = f1; al2p[q] = f2;
+                        const bool z = finite4(nb, nc, nd, ny);
+                        zrow = zrow && z; zdrow = zdrow && z;
+                    } else {
+                        row_b(q, k, hasL, hasR, a1pre, a2pre);
+                    }
+                }
+            }
+        } else if (kZero && ztile) {
             // zero state: aT, eT of both neighbours and a, e of row i are
             // zeros, so are a1, d1, b2, e2 (for finite f1, f2), and the b and
             // d sums reduce to one term
@@ -318,7 +372,8 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                         sb[k] = nb; sc[k] = nc; sd[k] = nd; sy[k] = ny;
                         sa[k] = szero(a1s); se[k] = szero(e2s);
                         al1p[q] = f1; al2p[q] = f2;
-                        zrow = zrow && finite4(nb, nc, nd, ny);
+                        const bool z = finite4(nb, nc, nd, ny);
+                        zrow = zrow && z; zdrow = zdrow && z && !nz(nd);
                     } else {
                         row_b(q, k, hasL, hasR, a1pre, a2pre);
                     }
@@ -338,7 +393,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                 }
             }
         }
-        if constexpr (kZero) ztile = __syncthreads_and(zrow);
+        if constexpr (kZero) { ztile = __syncthreads_and(zrow); zdtile = __syncthreads_and(zdrow); }
         else __syncthreads();
     }
 

@@ -69,12 +69,15 @@ def mp_candidates():
         yield dict(smem_rows=2 * cap, fuse_strides=fuse)
 
 
-def tune(budget_s: float = 600.0, verbose: bool = True):
+def tune(budget_s: float = 600.0, verbose: bool = True, only=None):
+    """Times the candidates of both paths (or of `only`: "f64" or "mixed")."""
     import torch
     t_start = time.time()
     rec = {"device": torch.cuda.get_device_name(0), "f64": [], "mixed": []}
     for kind, classes, cands, solver in (("f64", F64_CLASSES, list(f64_candidates()), solve_f64),
                                          ("mixed", MP_CLASSES, list(mp_candidates()), solve_mixed)):
+        if only and kind != only:
+            continue
         for n_max, m in classes:
             n = n_max if n_max <= 131072 else n_max // 2
             arrs = _batch(m, n)
@@ -138,8 +141,18 @@ def main():
     ap.add_argument("--header", default=os.path.join(CSRC, "tuned_params.h"))
     ap.add_argument("--write", action="store_true")
     ap.add_argument("--budget", type=float, default=600.0)
+    ap.add_argument("--only", choices=("f64", "mixed"), default=None,
+                    help="tune one path; the other's results come from --prev")
+    ap.add_argument("--prev", default=None, help="earlier JSON record (with --only)")
     args = ap.parse_args()
-    rec = tune(args.budget)
+    rec = tune(args.budget, only=args.only)
+    if args.only:
+        if not args.prev:
+            ap.error("--only needs --prev, the record that holds the other path's results")
+        with open(args.prev) as f:
+            prev = json.load(f)
+        other = "mixed" if args.only == "f64" else "f64"
+        rec[other], rec[other + "_best"] = prev[other], prev[other + "_best"]
     if args.json:
         with open(args.json, "w") as f:
             json.dump(rec, f, indent=1)
