@@ -178,12 +178,18 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
             for (int k = 0; k < NSTATE; k++) bufs[u][k] = base + ((size_t)u * NSTATE + k) * (size_t)(m * n);
     }
 
-    // global passes: K strides each, windows of L rows plus 2*(2^K-1) halo rows
+    // global passes: K strides each, windows of L rows plus 2*(2^K-1) halo rows.
+    // The s1 strides are spread evenly over the ceil(s1/fuse) passes (3+2+2,
+    // not 3+3+1: a one-stride pass spreads a pass's fixed costs over little
+    // work), and a pass of fewer strides turns the halo rows it does not need
+    // into tile rows.
+    const int npass = s1 > 0 ? (s1 + pl.fuse - 1) / pl.fuse : 0;
     int done = 0, cur = 0;
-    while (done < s1) {
-        const int K = std::min(pl.fuse, s1 - done);
+    for (int ip = 0; ip < npass; ip++) {
+        const int K = s1 / npass + (ip < s1 % npass ? 1 : 0);
         const int H = 2 * ((1 << K) - 1);
-        int L = pl.tile_rows > 0 ? pl.tile_rows : 1024;
+        const int Hfuse = 2 * ((1 << std::min(pl.fuse, s1)) - 1);
+        int L = (pl.tile_rows > 0 ? pl.tile_rows : 1024) + 2 * (Hfuse - H);
         if (L + 2 * H > pcr_max_smem_rows()) L = pcr_max_smem_rows() - 2 * H;
         if (L < 1) return set_error(PCRP_EINVAL, "%s: fuse_strides=%d leaves no tile rows", who, K);
         const int64_t nrmax = ceil_div(n, p.G);
