@@ -79,7 +79,8 @@ def fp64_ops(n: int):
 
 
 CONFIGS = {
-    "c0": dict(m=1024, n=512, kind=0, name="plain FP64 PCR, shared-memory path, m=1024 n=512"),
+    "c0": dict(m=1024, n=512, kind=0, layout="interleaved",
+               name="plain FP64 PCR, shared-memory path, m=1024 n=512, interleaved layout"),
     "c1": dict(m=256, n=65536, kind=0, name="plain FP64 PCR, global tile-splitting path, m=256 n=65536"),
     "c2": dict(m=4096, n=4096, kind=1, name="ADI convection-diffusion, m=4096 n=4096"),
     "c4": dict(m=64, n=1 << 20, kind=2, name="weakly dominant, m=64 n=2^20"),
@@ -161,26 +162,35 @@ def dist_setup(args):
     return world, rank, local, pg
 
 
-def cpu_sample_gunk(cfg, systems: int, reps: int = 1, solver: str = "pcr"):
+def cfg_layout(cfg):
+    """The workload's batch layout: interleaved (row-major over systems) or contiguous."""
+    import pcrp
+    return pcrp.INTERLEAVED if cfg.get("layout") == "interleaved" else pcrp.CONTIGUOUS
+
+
+def cpu_sample_gunk(cfg, systems: int, min_s: float = 2.0, solver: str = "pcr"):
     """Oracle PCR restatement (or, solver="ge", the FP64 banded Gaussian
-    elimination) on `systems` systems of the workload, all cores."""
+    elimination) on `systems` systems of the workload, in its layout, all
+    cores; the sample is solved again until min_s seconds of wall time have
+    accumulated.  Returns (Gunknowns/s, cores, seconds, repetitions)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     import pcrp
     m, n = systems, cfg["n"]
-    arrs = pcrp.generate(cfg["kind"], 7, m, n)
+    lay = cfg_layout(cfg)
+    arrs = pcrp.generate(cfg["kind"], 7, m, n, lay)
     O.lib()
     cores = os.cpu_count() or 1
-    best = None
-    for _ in range(reps):
+    total, reps = 0.0, 0
+    while total < min_s or reps == 0:
         t = time.perf_counter()
         if solver == "ge":
-            O.ge(*arrs, m, n, threads=cores)
+            O.ge(*arrs, m, n, lay, threads=cores)
         else:
-            O.pcr(*arrs, m, n, threads=cores)
-        dt = time.perf_counter() - t
-        best = dt if best is None else min(best, dt)
-    return m * n / best / 1e9, cores, best
+            O.pcr(*arrs, m, n, lay, threads=cores)
+        total += time.perf_counter() - t
+        reps += 1
+    return reps * m * n / total / 1e9, cores, total, reps
 
 
 def run_reference(args, world, rank):
@@ -191,18 +201,20 @@ def run_reference(args, world, rank):
     systems = max(1, min(cfg["m"], args.ref_systems))
     vals = []
     cores = os.cpu_count() or 1
+    reps = 1
     for k in range(args.warmup + args.steps):
-        v, cores, dt = cpu_sample_gunk(cfg, systems)
+        v, cores, dt, reps = cpu_sample_gunk(cfg, systems, min_s=0.5 if k < args.warmup else 2.0)
         if k >= args.warmup:
             vals.append(v)
     value = statistics.median(vals)
-    sample = f"{systems} of {cfg['m']} systems (n={cfg['n']}) per step, {cores} host threads"
+    sample = (f"{systems} of {cfg['m']} systems (n={cfg['n']}) solved {reps}x (>= 2 s) per step, "
+              f"{cores} host threads")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": cfg["m"] * cfg["n"] / value / 1e6,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded counter-based generator)", "impl": "reference",
-        "config": {"workload": cfg["name"], "m": cfg["m"], "n": cfg["n"], "layout": "contiguous",
+        "config": {"workload": cfg["name"], "m": cfg["m"], "n": cfg["n"], "layout": cfg.get("layout", "contiguous"),
                    "solver": "CPU restatement of the reference PCR-Penta (oracle/pcrp_oracle.c)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -224,14 +236,19 @@ def run_ours(args, world, rank, local, pg):
 
     # inputs: this rank's shard of systems (weak scaling: m systems per GPU)
     seed = 7 + rank
+    lay = cfg_layout(cfg)
     arrs = [torch.empty(m * n, dtype=torch.float64, device=dev) for _ in range(6)]
     with torch.cuda.stream(stream):
-        pcrp.generate_device(cfg["kind"], seed, m, n, pcrp.CONTIGUOUS, arrs, stream=stream)
+        pcrp.generate_device(cfg["kind"], seed, m, n, lay, arrs, stream=stream)
         rhs = arrs[5].clone()
     stream.synchronize()
     opts = pcrp.Opts(**json.loads(args.opts)) if args.opts else None
-    solve = (lambda: pcrp.solve_f64(*arrs, m, n, stream=stream, opts=opts)) if args.solver == "f64" else \
-        (lambda: pcrp.solve_mixed(*arrs, m, n, stream=stream, report=False, opts=opts))
+    solve = (lambda: pcrp.solve_f64(*arrs, m, n, lay, stream=stream, opts=opts)) if args.solver == "f64" else \
+        (lambda: pcrp.solve_mixed(*arrs, m, n, lay, stream=stream, report=False, opts=opts))
+
+    def first_systems(v, k):
+        """The first k systems of a batch array, contiguous (for host checks)."""
+        return v[: k * n] if lay == pcrp.CONTIGUOUS else v.view(n, m).t()[:k].contiguous().view(-1)
 
     def step():
         arrs[5].copy_(rhs, non_blocking=True)
@@ -324,8 +341,8 @@ def run_ours(args, world, rank, local, pg):
     other = None
     if args.compare:
         other_solver = "mixed" if args.solver == "f64" else "f64"
-        osolve = (lambda: pcrp.solve_mixed(*arrs, m, n, stream=stream, report=False)) if other_solver == "mixed" \
-            else (lambda: pcrp.solve_f64(*arrs, m, n, stream=stream))
+        osolve = (lambda: pcrp.solve_mixed(*arrs, m, n, lay, stream=stream, report=False)) if other_solver == "mixed" \
+            else (lambda: pcrp.solve_f64(*arrs, m, n, lay, stream=stream))
         oms = []
         with torch.cuda.stream(stream):
             for it in range(max(3, args.steps) + 2):
@@ -343,10 +360,10 @@ def run_ours(args, world, rank, local, pg):
         # mixed: the library's own report (sweeps, estimate, final residual) on one solve
         with torch.cuda.stream(stream):
             arrs[5].copy_(rhs, non_blocking=True)
-            info = pcrp.solve_mixed(*arrs, m, n, stream=stream, report=True)
+            info = pcrp.solve_mixed(*arrs, m, n, lay, stream=stream, report=True)
         other["mixed_report"] = {"sweeps": info.sweeps, "converged": info.converged,
                                  "fwd_err_est": info.fwd_err_est, "resid": info.resid}
-        x_mixed = arrs[5][: min(m, 16) * n].cpu().numpy()
+        x_mixed = first_systems(arrs[5], min(m, 16)).cpu().numpy()
         other["ratio_mixed_over_f64"] = (other["value"] / (world * m * n / (kms_med * 1e-3) / 1e9)
                                          if other_solver == "mixed" else
                                          (world * m * n / (kms_med * 1e-3) / 1e9) / other["value"])
@@ -357,7 +374,8 @@ def run_ours(args, world, rank, local, pg):
     lib_cmp = None
     if args.cusparse:
         import pcrp.compare as cmpmod
-        inter = [v.view(m, n).t().contiguous().view(-1) for v in arrs[:5]] + [rhs.view(m, n).t().contiguous().view(-1)]
+        inter = ([v.view(m, n).t().contiguous().view(-1) for v in arrs[:5]] + [rhs.view(m, n).t().contiguous().view(-1)]
+                 if lay == pcrp.CONTIGUOUS else list(arrs[:5]) + [rhs])
         work = [torch.empty_like(v) for v in inter]
         import ctypes
         L = cmpmod.lib()
@@ -388,12 +406,12 @@ def run_ours(args, world, rank, local, pg):
     # that overlap the solves; y is solved in place (the next step's rhs is the
     # previous solution, same work)
     h_in = [torch.empty(m * n, dtype=torch.float64, pin_memory=True) for _ in range(6)]
-    pcrp.generate_into(cfg["kind"], seed, m, n, pcrp.CONTIGUOUS, h_in)
+    pcrp.generate_into(cfg["kind"], seed, m, n, lay, h_in)
     e_steps = max(2, min(args.steps, 5))
     precision = 0 if args.solver == "f64" else 1
 
     def e2e_step():
-        pcrp.solve_host(*h_in, m, n, precision=precision, stream=stream)
+        pcrp.solve_host(*h_in, m, n, lay, precision=precision, stream=stream)
 
     with torch.cuda.stream(stream):
         e2e_step()
@@ -421,7 +439,7 @@ def run_ours(args, world, rank, local, pg):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.solver == "f64" else "f32+f64",
         "data": "synthetic (seeded counter-based generator, generated on device)",
-        "config": {"workload": cfg["name"], "m": m, "n": n, "layout": "contiguous",
+        "config": {"workload": cfg["name"], "m": m, "n": n, "layout": cfg.get("layout", "contiguous"),
                    "solver": "pcrp_solve_f64 (bit-faithful PCR-Penta)" if args.solver == "f64"
                    else "pcrp_solve_mixed (FP32 block PCR + FP64 refinement)",
                    "l2": (f"inputs ({48 * m * n / 1e6:.0f} MB) smaller than twice L2: a {2 * l2 / 1e6:.0f} MB "
@@ -461,16 +479,16 @@ def run_ours(args, world, rank, local, pg):
                 line["library_baseline"]["fwd_err_vs_ge"] = float((np.abs(xc64 - xg64).max(axis=1) /
                                                                    np.maximum(np.abs(xg64).max(axis=1), 1e-300)).max())
             line["compare"]["fwd_err_sample"] = f"first {ms} systems vs FP64 banded elimination"
-        v, cores, dt = cpu_sample_gunk(cfg, min(m, args.ref_systems))
+        v, cores, dt, reps = cpu_sample_gunk(cfg, min(m, args.ref_systems))
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": f"{min(m, args.ref_systems)} of {m} systems (n={n}), "
+                                "sample": f"{min(m, args.ref_systems)} of {m} systems (n={n}) solved {reps}x, "
                                           f"oracle PCR restatement, {dt:.2f} s wall"}
         # the FP64 host solver the accuracy is judged against: banded
         # Gaussian elimination, threads over systems (a reported baseline)
-        gv, gcores, gdt = cpu_sample_gunk(cfg, min(m, args.ref_systems), reps=2, solver="ge")
+        gv, gcores, gdt, greps = cpu_sample_gunk(cfg, min(m, args.ref_systems), solver="ge")
         line["host_ge"] = {"value": gv, "unit": UNIT, "cores": gcores,
-                           "sample": f"{min(m, args.ref_systems)} of {m} systems (n={n}), FP64 banded "
-                                     f"Gaussian elimination (oracle), {gdt:.3f} s wall"}
+                           "sample": f"{min(m, args.ref_systems)} of {m} systems (n={n}) solved {greps}x, "
+                                     f"FP64 banded Gaussian elimination (oracle), {gdt:.2f} s wall"}
     print(json.dumps(line), flush=True)
 
 
