@@ -318,6 +318,25 @@ def run_ours(args, world, rank, local, pg):
     kms_med = statistics.median(kms)
     achieved = BYTES_PER_UNKNOWN * m * n / (kms_med * 1e-3) / 1e9
 
+    # accuracy of the headline solve: x of one solve, its normwise residual
+    # ||y - A x||_inf / (||A||_inf ||x||_inf) per system on the GPU (worst
+    # system), and (below, with the host oracle) its forward error
+    with torch.cuda.stream(stream):
+        arrs[5].copy_(rhs, non_blocking=True)
+        solve()
+        x_head = arrs[5].clone()
+        r_head = torch.empty_like(x_head)
+        pcrp.residual_f64(*arrs[:5], rhs, x_head, r_head, m, n, lay, stream=stream)
+    stream.synchronize()
+
+    def per_sys(v):
+        return v.view(m, n) if lay == pcrp.CONTIGUOUS else v.view(n, m).t()
+    a_norm = sum(per_sys(v).abs() for v in arrs[:5]).amax(dim=1)
+    resid = float((per_sys(r_head).abs().amax(dim=1) /
+                   (a_norm * per_sys(x_head).abs().amax(dim=1)).clamp_min(1e-300)).max())
+    x_head16 = first_systems(x_head, min(m, 16)).cpu().numpy()
+    del r_head, x_head
+
     # FP64-pipe roofline of the faithful path: its FP64 operations at this
     # GPU's measured DFMA and division rates, against the kernel time
     fp64_roof = None
@@ -456,6 +475,7 @@ def run_ours(args, world, rank, local, pg):
                              f"({kms_med:.3f} ms); peak {peak_kind}"},
         "clocks": clk.summary(),
     }
+    line["accuracy"] = {"resid": resid, "resid_sample": f"all {m} systems, worst system"}
     if fp64_roof is not None:
         line["fp64_roofline"] = fp64_roof
     if other is not None:
@@ -463,22 +483,27 @@ def run_ours(args, world, rank, local, pg):
     if lib_cmp is not None:
         line["library_baseline"] = lib_cmp
     if args.cpu_baseline and world == 1:
+        # forward error of the headline solve and of the comparison points
+        # against FP64 banded elimination on the first systems
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        ms = min(m, 16)
+        host = pcrp.generate(cfg["kind"], seed, ms, n)
+        x_ge = O.ge(*host, ms, n)
+        xg64 = np.asarray(x_ge, dtype=np.float64).reshape(ms, n)
+        xh64 = np.asarray(x_head16, dtype=np.float64).reshape(ms, n)
+        line["accuracy"]["fwd_err_vs_ge"] = float((np.abs(xh64 - xg64).max(axis=1) /
+                                                   np.maximum(np.abs(xg64).max(axis=1), 1e-300)).max())
+        line["accuracy"]["fwd_err_sample"] = f"first {ms} systems vs FP64 banded elimination (oracle)"
         if other is not None:
-            # check the mixed solution against FP64 elimination on the first systems
-            sys.path.insert(0, os.path.join(ROOT, "oracle"))
-            import oracle as O
-            ms = min(m, 16)
-            host = pcrp.generate(cfg["kind"], seed, ms, n)
-            x_ge = O.ge(*host, ms, n)
             xm64 = np.asarray(x_mixed, dtype=np.float64).reshape(ms, n)
-            xg64 = np.asarray(x_ge, dtype=np.float64).reshape(ms, n)
             line["compare"]["fwd_err_vs_ge"] = float((np.abs(xm64 - xg64).max(axis=1) /
                                                       np.maximum(np.abs(xg64).max(axis=1), 1e-300)).max())
-            if lib_cmp is not None:
-                xc64 = np.asarray(x_gpsv, dtype=np.float64).reshape(ms, n)
-                line["library_baseline"]["fwd_err_vs_ge"] = float((np.abs(xc64 - xg64).max(axis=1) /
-                                                                   np.maximum(np.abs(xg64).max(axis=1), 1e-300)).max())
             line["compare"]["fwd_err_sample"] = f"first {ms} systems vs FP64 banded elimination"
+        if lib_cmp is not None:
+            xc64 = np.asarray(x_gpsv, dtype=np.float64).reshape(ms, n)
+            line["library_baseline"]["fwd_err_vs_ge"] = float((np.abs(xc64 - xg64).max(axis=1) /
+                                                               np.maximum(np.abs(xg64).max(axis=1), 1e-300)).max())
         v, cores, dt, reps = cpu_sample_gunk(cfg, min(m, args.ref_systems))
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"{min(m, args.ref_systems)} of {m} systems (n={n}) solved {reps}x, "
