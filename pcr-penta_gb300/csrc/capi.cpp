@@ -184,7 +184,7 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
     // work), and a pass of fewer strides turns the halo rows it does not need
     // into tile rows.
     const int npass = s1 > 0 ? (s1 + pl.fuse - 1) / pl.fuse : 0;
-    int done = 0, cur = 0;
+    int cur = 0;
     for (int ip = 0; ip < npass; ip++) {
         const int K = s1 / npass + (ip < s1 % npass ? 1 : 0);
         const int H = 2 * ((1 << K) - 1);
@@ -206,7 +206,6 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
         for (int k = 0; k < NSTATE; k++) p.src[k] = bufs[cur][k];
         p.src_ss = n; p.src_rs = 1;
         cur ^= 1;
-        done += K;
         p.G <<= K;
     }
 
