@@ -18,15 +18,18 @@ def dd_bands(rng, m, n, garbage=False):
     return [v.ravel().copy() for v in (a, b, c, d, e, y)]
 
 
-def zero_bands(rng, m, n, special=False):
+def zero_bands(rng, m, n, special=False, zero_d=False):
     """Batch whose outer bands a, e are zeros of random sign (a pentadiagonal
     system already in the state of the late strides, where every product of
     the multipliers has a zero factor), with zeros of random sign sprinkled
-    into b, d and y; `special` adds +-inf and NaN entries to a few systems."""
+    into b, d and y; `zero_d` makes d all zeros of random sign too (the lower
+    bidiagonal state); `special` adds +-inf and NaN entries to a few systems."""
     def signed_zeros(shape):
         return np.where(rng.random(shape) < 0.5, 0.0, -0.0)
     a, e = signed_zeros((m, n)), signed_zeros((m, n))
     b, d, y = [rng.uniform(-1, 1, (m, n)) for _ in range(3)]
+    if zero_d:
+        d = signed_zeros((m, n))
     for arr in (b, d, y):
         hit = rng.random((m, n)) < 0.05
         arr[hit] = signed_zeros(int(hit.sum()))

@@ -95,19 +95,21 @@ def test_adi_and_toeplitz_bitexact(cuda):
     (300, "auto", pcrp.Opts(smem_rows=8, fuse_strides=3, tile_rows=7)),
     (65536, "auto", None)])
 @pytest.mark.parametrize("special", [False, True])
-def test_zero_outer_bands_bitexact(cuda, n, path, opts, special):
-    """Zero outer bands (signed zeros), zeros in b, d, y, and +-inf / NaN
-    entries: the rows whose products have zero factors are formed on the
-    integer pipe and must give the bits of the IEEE operations, zero signs
-    included; rows with a non-finite operand take the FP64 operations."""
-    rng = np.random.default_rng(n + 7 * special)
+@pytest.mark.parametrize("zero_d", [False, True])
+def test_zero_outer_bands_bitexact(cuda, n, path, opts, special, zero_d):
+    """Zero outer bands (signed zeros), zeros in b, d, y (or d all zeros: the
+    lower-bidiagonal state), and +-inf / NaN entries: the rows whose products
+    have zero factors are formed on the integer pipe and must give the bits
+    of the IEEE operations, zero signs included; rows with a non-finite
+    operand take the FP64 operations."""
+    rng = np.random.default_rng(n + 7 * special + 13 * zero_d)
     m = 6
-    arrs = zero_bands(rng, m, n, special=special)
+    arrs = zero_bands(rng, m, n, special=special, zero_d=zero_d)
     x, _ = gpu_f64(arrs, m, n, path=path, opts=opts)
     ref = O.pcr(*arrs, m, n)
-    if not special:
+    if not special and not zero_d:
         assert np.isfinite(ref).all()
-    assert_bitexact(x, ref, f"zero bands n={n} path={path} special={special}")
+    assert_bitexact(x, ref, f"zero bands n={n} path={path} special={special} zero_d={zero_d}")
 
 
 def test_bands_are_not_modified(cuda):
