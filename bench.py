@@ -420,6 +420,39 @@ def run_ours(args, world, rank, local, pg):
         x_gpsv = work[5].view(n, m).t()[: min(m, 16)].contiguous().view(-1).cpu().numpy()
         del inter, work, gbuf
 
+    # the headline solver on the same systems in the other batch layout
+    # (contiguous <-> interleaved), and whether its solution has the same bits
+    alt_layout = None
+    if args.other_layout:
+        alt_lay = pcrp.INTERLEAVED if lay == pcrp.CONTIGUOUS else pcrp.CONTIGUOUS
+
+        def relayout(v):
+            return (v.view(m, n).t() if lay == pcrp.CONTIGUOUS else v.view(n, m).t()).contiguous().view(-1)
+        alt = [relayout(v) for v in arrs[:5]] + [torch.empty_like(rhs)]
+        alt_rhs = relayout(rhs)
+        asolve = (lambda: pcrp.solve_f64(*alt, m, n, alt_lay, stream=stream, opts=opts)) if args.solver == "f64" \
+            else (lambda: pcrp.solve_mixed(*alt, m, n, alt_lay, stream=stream, report=False, opts=opts))
+        ams = []
+        with torch.cuda.stream(stream):
+            for it in range(max(3, args.steps) + 1):
+                alt[5].copy_(alt_rhs, non_blocking=True)
+                if small:
+                    flush.zero_()
+                ek0.record(stream)
+                asolve()
+                ek1.record(stream)
+                ek1.synchronize()
+                if it >= 1:
+                    ams.append(ek0.elapsed_time(ek1))
+        x_alt = (alt[5].view(m, n) if alt_lay == pcrp.CONTIGUOUS else alt[5].view(n, m).t())[: min(m, 16)]
+        same = bool(torch.equal(x_alt.contiguous().view(-1).cpu().view(torch.int64),
+                                torch.from_numpy(x_head16).view(torch.int64)))
+        alt_layout = {"layout": "interleaved" if alt_lay == pcrp.INTERLEAVED else "contiguous",
+                      "ms_per_solve": statistics.median(ams),
+                      "value": world * m * n / (statistics.median(ams) * 1e-3) / 1e9,
+                      "same_bits_as_headline": same, "checked": f"first {min(m, 16)} systems"}
+        del alt, alt_rhs
+
     # end to end through the public API with host buffers (pinned): pcrp_solve_host
     # copies each step's six input arrays in and the solution out, in chunks
     # that overlap the solves; y is solved in place (the next step's rhs is the
@@ -482,6 +515,8 @@ def run_ours(args, world, rank, local, pg):
         line["compare"] = other
     if lib_cmp is not None:
         line["library_baseline"] = lib_cmp
+    if alt_layout is not None:
+        line["other_layout"] = alt_layout
     if args.cpu_baseline and world == 1:
         # forward error of the headline solve and of the comparison points
         # against FP64 banded elimination on the first systems
@@ -599,6 +634,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-cusparse", dest="cusparse", action="store_false",
                     help="skip timing cuSPARSE gpsvInterleavedBatch on the same systems")
+    ap.add_argument("--no-other-layout", dest="other_layout", action="store_false",
+                    help="skip the headline solver on the same systems in the other batch layout")
     ap.add_argument("--no-compare", dest="compare", action="store_false",
                     help="skip timing the other precision on the same inputs")
     args = ap.parse_args()

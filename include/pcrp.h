@@ -153,7 +153,10 @@ pcrp_status pcrp_solve_f64_noalloc(const double* a, const double* b, const doubl
  * call is asynchronous and never reports PCRP_ENOCONV.  From the second
  * asynchronous call with the same arguments and workspace the sweeps run as
  * a CUDA graph whose while node stops at convergence (environment variable
- * PCRP_NO_GRAPH: always host-driven launches).
+ * PCRP_NO_GRAPH: always host-driven launches).  An interleaved batch of more
+ * than one system is transposed into contiguous copies in the workspace,
+ * solved there and transposed back (same result bits as the contiguous solve;
+ * pcrp_workspace_size counts the copies).
  * No counterpart in the reference (new work named by the solver's design). */
 pcrp_status pcrp_solve_mixed(const double* a, const double* b, const double* c,
                              const double* d, const double* e, double* y,

@@ -124,7 +124,7 @@ static int split_strides(int64_t n, int smem_rows)
     return s;
 }
 
-size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_sweeps, bool info);
+size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_sweeps, bool info, int32_t layout);
 
 size_t f64_workspace_bytes(int64_t m, int64_t n, int32_t layout, const F64Plan& pl, bool split)
 {
@@ -260,7 +260,7 @@ pcrp_status pcrp_workspace_size(int64_t m, int64_t n, int32_t layout, int32_t wh
     const F64Plan pl = f64_plan(opts, n);
     switch (which) {
     case 0: *bytes = f64_workspace_bytes(m, n, layout, pl, true); return PCRP_OK;
-    case 1: *bytes = mixed_workspace_bytes(m, n, opts, 64, true); return PCRP_OK;
+    case 1: *bytes = mixed_workspace_bytes(m, n, opts, 64, true, layout); return PCRP_OK;
     default: return set_error(PCRP_EINVAL, "pcrp_workspace_size: unknown entry family %d", which);
     }
 }

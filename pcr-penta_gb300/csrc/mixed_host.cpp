@@ -339,11 +339,16 @@ pcrp_status launch_sweep_graph(const MpArgs& A, const SweepPlan& S, cudaStream_t
 
 }  // namespace
 
-size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_sweeps, bool info)
+// Contiguous copies of the six arrays for the layout adapter of an
+// interleaved batch (m > 1), after the solver's own workspace.
+static size_t adapter_array_bytes(int64_t m, int64_t n) { return ((size_t)m * n * sizeof(double) + 255) / 256 * 256; }
+static bool adapts(int32_t layout, int64_t m) { return layout == PCRP_LAYOUT_INTERLEAVED && m > 1; }
+
+size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_sweeps, bool info, int32_t layout)
 {
     if (m <= 0 || n <= 0) return 0;
     const MpPlan pl = mp_plan((n + 1) / 2, o);
-    return mp_layout(m, n, max_sweeps, pl, info).total;
+    return mp_layout(m, n, max_sweeps, pl, info).total + (adapts(layout, m) ? 6 * adapter_array_bytes(m, n) : 0);
 }
 
 // Enqueues prep + max_sweeps refinement sweeps of a uniform batch on `st`
@@ -471,18 +476,42 @@ extern "C" pcrp_status pcrp_solve_mixed(const double* a, const double* b, const 
     const MpPlan pl = mp_plan(nb, opts);
     if (pl.npass > kMpMaxPasses) return set_error(PCRP_EINVAL, "%s: n too large for the pass plan", who);
     const MpLayout WL = mp_layout(m, n, max_sweeps, pl, info != nullptr);
+    // Layout adapter: the window kernels walk along a system, which in the
+    // interleaved layout means loads m doubles apart.  An interleaved batch
+    // (m > 1) is transposed into contiguous copies in the workspace, solved
+    // there, and the solution transposed back into y.
+    const bool adapt = adapts(layout, m);
+    const size_t arr = adapter_array_bytes(m, n);
     void* ws = nullptr;
-    pcrp_status rc = get_workspace(opts, WL.total, st, &ws);
+    pcrp_status rc = get_workspace(opts, WL.total + (adapt ? 6 * arr : 0), st, &ws);
     if (rc != PCRP_OK) return rc;
     char* base = static_cast<char*>(ws);
     auto U = [&](size_t off) { return reinterpret_cast<unsigned*>(base + off); };
-    MpArgs A{};
-    rc = mixed_enqueue(a, b, c, d, e, y, m, n, layout == PCRP_LAYOUT_CONTIGUOUS ? n : 1,
-                       layout == PCRP_LAYOUT_CONTIGUOUS ? 1 : m, tol, max_sweeps, opts, info != nullptr, ws, st, &A);
-    if (rc != PCRP_OK) return rc;
     cudaError_t ce;
+    const double* src[6] = {a, b, c, d, e, y};
+    double* cpy[6] = {};
+    int64_t ss = layout == PCRP_LAYOUT_CONTIGUOUS ? n : 1, rs = layout == PCRP_LAYOUT_CONTIGUOUS ? 1 : m;
+    if (adapt) {
+        for (int k = 0; k < 6; k++)
+            if (src[k]) cpy[k] = reinterpret_cast<double*>(base + WL.total + k * arr);
+        ce = launch_transpose(src, cpy, 6, n, m, st);
+        if (ce != cudaSuccess) return cuda_error(ce, "layout adapter (interleaved -> contiguous)");
+        a = cpy[0]; b = cpy[1]; c = cpy[2]; d = cpy[3]; e = cpy[4];
+        ss = n; rs = 1;
+    }
+    double* ys = adapt ? cpy[5] : y;             // the solver's y: the copy, or y itself
+    MpArgs A{};
+    rc = mixed_enqueue(a, b, c, d, e, ys, m, n, ss, rs, tol, max_sweeps, opts, info != nullptr, ws, st, &A);
+    if (rc != PCRP_OK) return rc;
+    auto adapt_out = [&]() -> pcrp_status {
+        if (!adapt) return PCRP_OK;
+        const double* from[1] = {ys};
+        double* to[1] = {y};
+        cudaError_t te = launch_transpose(from, to, 1, m, n, st);
+        return te == cudaSuccess ? PCRP_OK : cuda_error(te, "layout adapter (contiguous -> interleaved)");
+    };
 
-    if (!info) return PCRP_OK;
+    if (!info) return adapt_out();
 
     // report: y still holds the rhs (the iterate was kept in X); final
     // residual r = y - A X, its norms, then X -> y
@@ -490,10 +519,12 @@ extern "C" pcrp_status pcrp_solve_mixed(const double* a, const double* b, const 
     unsigned* rn = U(WL.rn);
     ce = cudaMemsetAsync(rn, 0, 3 * m * sizeof(unsigned), st);
     if (ce != cudaSuccess) return cuda_error(ce, "cudaMemsetAsync");
-    ce = launch_residual(a, b, c, d, e, y, A.Xout, rb, m, n, A.ss, A.rs, n, 1, st);
+    ce = launch_residual(a, b, c, d, e, ys, A.Xout, rb, m, n, A.ss, A.rs, n, 1, st);
     if (ce == cudaSuccess) ce = launch_resid_norm(a, b, c, d, e, A.Xout, rb, m, n, A.ss, A.rs, rn, rn + m, rn + 2 * m, st);
-    if (ce == cudaSuccess) ce = launch_copy_out(A.Xout, y, m, n, A.ss, A.rs, st);
+    if (ce == cudaSuccess) ce = launch_copy_out(A.Xout, ys, m, n, A.ss, A.rs, st);
     if (ce != cudaSuccess) return cuda_error(ce, "mixed report launch");
+    rc = adapt_out();
+    if (rc != PCRP_OK) return rc;
     std::vector<unsigned> norms(3 * m);
     ce = cudaMemcpyAsync(norms.data(), rn, 3 * m * sizeof(unsigned), cudaMemcpyDeviceToHost, st);
     if (ce != cudaSuccess) return cuda_error(ce, "mixed report copy");

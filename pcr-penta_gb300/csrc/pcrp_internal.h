@@ -60,6 +60,11 @@ struct PcrPassArgs {
 
 // Host-side launchers (pcr_f64.cu).
 cudaError_t launch_pcr_pass(const PcrPassArgs& p, int threads, cudaStream_t s);
+// dst[k] (cols x rows) = transpose of src[k] (rows x cols), both row-major,
+// for up to 6 arrays in one launch; pairs with a null pointer are skipped
+// (layout.cu): interleaved n x m <-> contiguous m x n batches
+cudaError_t launch_transpose(const double* const* src, double* const* dst, int narr, int64_t rows, int64_t cols,
+                             cudaStream_t s);
 size_t pcr_pass_smem_bytes(int TRmax);
 int pcr_max_smem_rows();
 

@@ -22,7 +22,7 @@
 namespace pcrp {
 
 pcrp_status get_workspace(const pcrp_opts* o, size_t bytes, cudaStream_t s, void** out);
-size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_sweeps, bool info);
+size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_sweeps, bool info, int32_t layout);
 pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, const double* d, const double* e,
                           double* y, int64_t m, int64_t n, int64_t ss, int64_t rs, double tol, int max_sweeps,
                           const pcrp_opts* opts, bool keep_x, void* ws, cudaStream_t st, MpArgs* out);
@@ -138,7 +138,7 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
         pad_off.push_back(per_class);
         per_class += r256((size_t)6 * ms * N * sizeof(double));
         mix_off.push_back(per_class);
-        per_class += r256(mixed_workspace_bytes(ms, N, o, max_sweeps, false));
+        per_class += r256(mixed_workspace_bytes(ms, N, o, max_sweeps, false, PCRP_LAYOUT_CONTIGUOUS));
     }
     const size_t lists = r256((size_t)nsys * sizeof(int64_t));
     const size_t total = lists + 256 + per_class;

@@ -109,3 +109,16 @@ def test_ragged_sizes(built_lib):
     # log-uniform: about half of the systems below the geometric mean
     gm = np.sqrt(32 * 65536)
     assert 0.4 < np.mean(s < gm) < 0.6
+
+
+def test_mixed_workspace_includes_layout_adapter(built_lib):
+    """Interleaved batches of more than one system are solved by the mixed
+    solver through contiguous copies of the six arrays in the workspace: the
+    size query counts them (256-byte aligned each); one system needs none."""
+    import pcrp
+    for m, n in ((4, 4096), (3, 1000), (256, 65536)):
+        arr = (m * n * 8 + 255) // 256 * 256
+        ci = pcrp.workspace_size(m, n, pcrp.CONTIGUOUS, which=1)
+        ii = pcrp.workspace_size(m, n, pcrp.INTERLEAVED, which=1)
+        assert ii - ci == 6 * arr
+    assert pcrp.workspace_size(1, 5000, pcrp.INTERLEAVED, which=1) == pcrp.workspace_size(1, 5000, pcrp.CONTIGUOUS, which=1)

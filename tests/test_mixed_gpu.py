@@ -259,3 +259,39 @@ def test_mixed_inside_a_caller_graph_capture(cuda, mode):
         torch.cuda.synchronize()
         host = [v.cpu().numpy() for v in fresh]
         assert O.fwd_err(arrs[5].cpu().numpy(), O.ge(*host, m, n), m, n) <= TOL
+
+
+@pytest.mark.parametrize("m,n", [(5, 512), (3, 4096), (4, 65536), (2, 1000)])
+def test_mixed_interleaved_adapter_matches_contiguous(cuda, m, n):
+    """An interleaved batch is solved through the layout adapter (transposed
+    into contiguous copies, solved, transposed back): the same bits as the
+    contiguous solve of the same systems, with and without the report, with
+    NULL outer bands too, and in a caller workspace sized by
+    pcrp_workspace_size for the interleaved layout."""
+    import torch
+    arrs = dd_bands(np.random.default_rng(m * n), m, n)
+    inter = to_layout(arrs, m, n, pcrp.INTERLEAVED)
+    xc, _, _ = run_mixed(arrs, m, n, pcrp.CONTIGUOUS, report=False)
+    for report in (False, True):
+        xi, _, _ = run_mixed(inter, m, n, pcrp.INTERLEAVED, report=report)
+        xi_c = np.ascontiguousarray(xi.reshape(n, m).T).ravel()
+        assert np.array_equal(xi_c.view(np.uint64), xc.view(np.uint64)), f"report={report}"
+    # tridiagonal: NULL outer bands through the adapter
+    tri = [np.zeros_like(arrs[0])] + list(arrs[1:4]) + [np.zeros_like(arrs[4]), arrs[5]]
+    tc = to_device(tri, "cuda:0")
+    pcrp.solve_mixed(None, *tc[1:4], None, tc[5], m, n, pcrp.CONTIGUOUS, report=False)
+    ti = to_device(to_layout(tri, m, n, pcrp.INTERLEAVED), "cuda:0")
+    pcrp.solve_mixed(None, *ti[1:4], None, ti[5], m, n, pcrp.INTERLEAVED, report=False)
+    torch.cuda.synchronize()
+    assert torch.equal(ti[5].view(n, m).t().contiguous().view(-1).view(torch.int64), tc[5].view(torch.int64))
+    # caller workspace: the interleaved size works, the contiguous one is refused
+    need = pcrp.workspace_size(m, n, pcrp.INTERLEAVED, which=1)
+    assert need > pcrp.workspace_size(m, n, pcrp.CONTIGUOUS, which=1)
+    ws = torch.empty(need, dtype=torch.uint8, device="cuda")
+    xw, _, _ = run_mixed(inter, m, n, pcrp.INTERLEAVED, report=True,
+                         opts=pcrp.Opts(workspace=ws.data_ptr(), workspace_bytes=need))
+    assert np.array_equal(np.ascontiguousarray(xw.reshape(n, m).T).ravel().view(np.uint64), xc.view(np.uint64))
+    small = pcrp.workspace_size(m, n, pcrp.CONTIGUOUS, which=1)
+    with pytest.raises(pcrp.PcrpError):
+        run_mixed(inter, m, n, pcrp.INTERLEAVED, report=True,
+                  opts=pcrp.Opts(workspace=ws.data_ptr(), workspace_bytes=small))
