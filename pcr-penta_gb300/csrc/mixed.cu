@@ -896,14 +896,12 @@ mp_xupdate_kernel(MpArgs p)
 // Per-system decision after sweep s from the norms of this sweep and the last.
 struct UpDecision { bool done, last; float est; };
 
-__device__ __forceinline__ UpDecision up_decide(const MpArgs& p, int64_t j)
+// The stopping rule after sweep s from the sweep's max |dx_s| (nd) and the
+// previous sweep's max |dx_{s-1}| (ndp) and max |x_{s-1}| (nxp).
+__device__ __forceinline__ UpDecision stop_rule(int s, float nd, float ndp, float nxp, float tol, int max_sweeps)
 {
-    const int s = p.sweep;
     UpDecision D{false, false, 0.0f};
     if (s >= 1) {
-        const float nd = __uint_as_float(p.ndx[(int64_t)s * p.m + j]);
-        const float ndp = __uint_as_float(p.ndx[(int64_t)(s - 1) * p.m + j]);
-        const float nxp = __uint_as_float(p.nx[(int64_t)(s - 1) * p.m + j]);
         if (nd == 0.0f) D.done = true;
         else if (ndp > 0.0f) {
             // Two ways to be done.  (1) The correction itself is below tol/2:
@@ -917,11 +915,20 @@ __device__ __forceinline__ UpDecision up_decide(const MpArgs& p, int64_t j)
             const float rho = nd / ndp;
             const float contr = rho < 0.5f ? 2.0f * rho / (1.0f - rho) * rel : rel;
             D.est = fminf(rel, contr);
-            D.done = rel <= 0.5f * p.tol || (rho < 0.5f && contr <= p.tol);
+            D.done = rel <= 0.5f * tol || (rho < 0.5f && contr <= tol);
         }
     }
-    D.last = D.done || s == p.max_sweeps - 1;
+    D.last = D.done || s == max_sweeps - 1;
     return D;
+}
+
+__device__ __forceinline__ UpDecision up_decide(const MpArgs& p, int64_t j)
+{
+    const int s = p.sweep;
+    if (s < 1) return stop_rule(s, 0.0f, 0.0f, 0.0f, p.tol, p.max_sweeps);
+    return stop_rule(s, __uint_as_float(p.ndx[(int64_t)s * p.m + j]),
+                     __uint_as_float(p.ndx[(int64_t)(s - 1) * p.m + j]),
+                     __uint_as_float(p.nx[(int64_t)(s - 1) * p.m + j]), p.tol, p.max_sweeps);
 }
 
 // One thread per system: a system that is done (or out of sweeps) finishes in
@@ -947,6 +954,125 @@ mp_decide_kernel(MpArgs p)
     const int cnt = __syncthreads_count(finish);
     if (threadIdx.x == 0 && cnt > 0)
         for (int s2 = s + 1; s2 <= p.max_sweeps; s2++) atomicSub(&p.live[s2], cnt);
+}
+
+// Systems that fit one shared-memory tile (every block row of a system in
+// one CTA): all sweeps of a system run inside its CTA, so nothing waits for
+// the rest of the batch between sweeps and the whole solve is one launch.
+// Per system:
+//  1. FP64 bands and y -> row-scaled, normalised FP32 blocks (prep_row): in
+//     shared memory for the first solve, and in S0, Mi for the later ones;
+//  2. per sweep: cyclic reduction to the top and back substitution (dx_s),
+//     x_s = x_{s-1} + dx_s in FP64 (X0, contiguous), the maxima of |dx_s| and
+//     |x_s| over the CTA, the stopping rule; if another sweep follows,
+//     r_s = y - A x_s in FP64, row-scaled and normalised into the tile's rhs,
+//     and the level-0 blocks back from S0 (the reduction overwrote them);
+//  3. x -> the output, status, sweeps and estimate.
+// y keeps the rhs until the final copy, so no copy of it is needed.
+__device__ __forceinline__ void block_max(unsigned& dmb, unsigned long long& xb, unsigned* red_d,
+                                          unsigned long long* red_x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dmb = max(dmb, __shfl_xor_sync(0xffffffffu, dmb, o));
+        xb = max(xb, __shfl_xor_sync(0xffffffffu, xb, o));
+    }
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0) { red_d[w] = dmb; red_x[w] = xb; }
+    __syncthreads();
+    dmb = 0u; xb = 0ull;
+    for (int k = 0; k < nw; k++) { dmb = max(dmb, red_d[k]); xb = max(xb, red_x[k]); }
+    __syncthreads();                              // the scratch is reused by the next call
+}
+
+__global__ void __launch_bounds__(kMpThreads)
+mp_small_kernel(MpArgs p)
+{
+    extern __shared__ float4 fsm[];
+    __shared__ unsigned red_d[kMpThreads / 32];
+    __shared__ unsigned long long red_x[kMpThreads / 32];
+    pdl_wait();
+    pdl_release();
+    const int64_t n = p.n, nb = (n + 1) / 2;
+    const int TR = (int)nb, TRs = mp_pass_rows(TR);
+    float4* sL = fsm;
+    float4* sU = fsm + TRs;
+    float2* sY = reinterpret_cast<float2*>(fsm + 2 * TRs);
+    const int tid = threadIdx.x, bd = blockDim.x;
+    for (int64_t j = blockIdx.x; j < p.m; j += gridDim.x) {
+        double* __restrict__ X = p.X0 + j * n;
+        for (int k = tid; k < TR; k += bd) {
+            const PrepRow r = prep_row(p, j, k);
+            const int64_t q = j * nb + k;
+            p.S0[2 * q] = f4(r.L);
+            p.S0[2 * q + 1] = f4(r.U);
+            p.Mi[q] = f4(r.Mi);
+            const int sk = swz(k);
+            sL[sk] = f4(r.L); sU[sk] = f4(r.U); sY[sk] = r.Y;
+        }
+        __syncthreads();
+        float ndp = 0.0f, nxp = 0.0f;
+        UpDecision D{false, false, 0.0f};
+        int s = 0;
+        for (;; s++) {
+            const int top = cr_reduce(sL, sU, sY, TR, 31, 0, TR);   // a whole system: never -1
+            cr_substitute(sL, sU, sY, TR, top);
+            unsigned dmb = 0u;
+            unsigned long long xb = 0ull;
+            for (int k = tid; k < TR; k += bd) {
+                const float2 v = sY[swz(k)];
+                const int64_t i0 = 2 * (int64_t)k;
+                const double x0 = s ? __dadd_rn(X[i0], f2d(v.x)) : f2d(v.x);
+                X[i0] = x0;
+                dmb = max(dmb, __float_as_uint(fabsf(v.x)));
+                xb = max(xb, absbits(x0));
+                if (i0 + 1 < n) {
+                    const double x1 = s ? __dadd_rn(X[i0 + 1], f2d(v.y)) : f2d(v.y);
+                    X[i0 + 1] = x1;
+                    dmb = max(dmb, __float_as_uint(fabsf(v.y)));
+                    xb = max(xb, absbits(x1));
+                }
+            }
+            block_max(dmb, xb, red_d, red_x);     // (its barriers also publish X to the CTA)
+            // non-negative floats order like their bits, a nan above everything
+            const float nd = __uint_as_float(dmb);
+            const float nx = d2f_scaled(__longlong_as_double((long long)xb), 0);
+            D = stop_rule(s, nd, ndp, nxp, p.tol, p.max_sweeps);
+            if (D.last) break;
+            ndp = nd; nxp = nx;
+            for (int k = tid; k < TR; k += bd) {
+                const int64_t i0 = 2 * (int64_t)k, q = j * nb + k;
+                const PairRow P = load_pair(p, j * p.ss, i0);
+                const double xm2 = i0 >= 2 ? X[i0 - 2] : 0.0, xm1 = i0 >= 1 ? X[i0 - 1] : 0.0, x0 = X[i0];
+                const double x1 = i0 + 1 < n ? X[i0 + 1] : 0.0, x2 = i0 + 2 < n ? X[i0 + 2] : 0.0;
+                const double x3 = i0 + 3 < n ? X[i0 + 3] : 0.0;
+                double r0 = fma(-P.c0, x0, P.y0);
+                if (p.a && i0 >= 2) r0 = fma(-P.a0, xm2, r0);
+                if (i0 >= 1) r0 = fma(-P.b0, xm1, r0);
+                if (i0 + 1 < n) r0 = fma(-P.d0, x1, r0);
+                if (p.e && i0 + 2 < n) r0 = fma(-P.e0, x2, r0);
+                const float rf0 = d2f_scaled(r0, d_exponent(P.c0));
+                float rf1 = 0.0f;                 // the identity row of an odd system's last block row
+                if (i0 + 1 < n) {
+                    double r1 = fma(-P.c1, x1, P.y1);
+                    if (p.a && i0 >= 1) r1 = fma(-P.a1, xm1, r1);
+                    r1 = fma(-P.b1, x0, r1);
+                    if (i0 + 2 < n) r1 = fma(-P.d1, x2, r1);
+                    if (p.e && i0 + 3 < n) r1 = fma(-P.e1, x3, r1);
+                    rf1 = d2f_scaled(r1, d_exponent(P.c1));
+                }
+                const float4 Mi = p.Mi[q];
+                const int sk = swz(k);
+                sY[sk] = make_float2(fmaf(Mi.x, rf0, Mi.y * rf1), fmaf(Mi.z, rf0, Mi.w * rf1));
+                sL[sk] = p.S0[2 * q];
+                sU[sk] = p.S0[2 * q + 1];
+            }
+            __syncthreads();
+        }
+        for (int64_t i = tid; i < n; i += bd) p.xout[j * p.oss + i * p.ors] = X[i];
+        if (tid == 0) { p.fin[j] = s + 1; p.status[j] = D.done ? 1 : 2; p.est[j] = D.est; }
+        __syncthreads();                          // the next system reuses the tile
+    }
 }
 
 // r_s = y - A x_s (FP64, FMA chain) for the systems still running, row-scaled
@@ -1196,6 +1322,21 @@ cudaError_t launch_mp_try(const MpPassArgs& p, cudaStream_t s)
     if (e != cudaSuccess) return e;
     const int64_t blocks = std::min<int64_t>(items, mp_grid_cap((const void*)mp_try_kernel, kMpTryThreads, smem));
     e = launch_dependent(mp_try_kernel, (unsigned)blocks, kMpTryThreads, smem, s, p);
+    count_launch();
+    return e;
+}
+
+cudaError_t launch_mp_small(const MpArgs& p, cudaStream_t s)
+{
+    const int64_t nb = (p.n + 1) / 2;
+    if (nb > kMpMaxRows) return cudaErrorInvalidValue;
+    if (p.m <= 0) return cudaSuccess;
+    const size_t smem = mp_pass_smem((int)nb);
+    cudaError_t e = cudaFuncSetAttribute(mp_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)mp_pass_smem(kMpMaxRows));
+    if (e != cudaSuccess) return e;
+    const int64_t blocks = std::min<int64_t>(p.m, mp_grid_cap((const void*)mp_small_kernel, kMpThreads, smem));
+    e = launch_dependent(mp_small_kernel, (unsigned)blocks, kMpThreads, smem, s, p);
     count_launch();
     return e;
 }

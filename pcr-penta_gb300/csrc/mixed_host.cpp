@@ -421,6 +421,14 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     S.P[1] = pl.npass > 1 ? F(WL.P1) : nullptr;
     A.ctr = reinterpret_cast<int*>(base + WL.ctr);
 
+    // Systems that fit one shared-memory tile: every sweep of a system in one
+    // CTA, the whole solve one launch (no sweep loop to drive)
+    if (pl.s1 == 0) {
+        if (out) *out = A;
+        const cudaError_t cs = launch_mp_small(A, st);
+        return cs == cudaSuccess ? PCRP_OK : cuda_error(cs, "mixed small-system launch");
+    }
+
     cudaError_t ce;
     const int gm = keep_x ? 0 : graph_mode(st);
     if (gm == 1) {

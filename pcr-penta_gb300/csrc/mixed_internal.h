@@ -120,6 +120,7 @@ cudaError_t launch_mp_init(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_first(const MpArgs& p, const MpWindows& g, cudaStream_t s);
 cudaError_t launch_mp_prep(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_pass(const MpPassArgs& p, cudaStream_t s);
+cudaError_t launch_mp_small(const MpArgs& p, cudaStream_t s);   // whole systems, every sweep in one CTA
 cudaError_t launch_mp_try(const MpPassArgs& p, cudaStream_t s);
 cudaError_t launch_mp_xupdate(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_decide(const MpArgs& p, cudaStream_t s);
