@@ -985,12 +985,14 @@ __device__ __forceinline__ void block_max(unsigned& dmb, unsigned long long& xb,
     __syncthreads();                              // the scratch is reused by the next call
 }
 
-__global__ void __launch_bounds__(kMpThreads)
+constexpr int kMpSmallThreadsMax = 512;          // systems of >= 1024 block rows: 512 threads
+
+__global__ void __launch_bounds__(kMpSmallThreadsMax, 2)
 mp_small_kernel(MpArgs p)
 {
     extern __shared__ float4 fsm[];
-    __shared__ unsigned red_d[kMpThreads / 32];
-    __shared__ unsigned long long red_x[kMpThreads / 32];
+    __shared__ unsigned red_d[kMpSmallThreadsMax / 32];
+    __shared__ unsigned long long red_x[kMpSmallThreadsMax / 32];
     pdl_wait();
     pdl_release();
     const int64_t n = p.n, nb = (n + 1) / 2;
@@ -1335,8 +1337,11 @@ cudaError_t launch_mp_small(const MpArgs& p, cudaStream_t s)
     cudaError_t e = cudaFuncSetAttribute(mp_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)mp_pass_smem(kMpMaxRows));
     if (e != cudaSuccess) return e;
-    const int64_t blocks = std::min<int64_t>(p.m, mp_grid_cap((const void*)mp_small_kernel, kMpThreads, smem));
-    e = launch_dependent(mp_small_kernel, (unsigned)blocks, kMpThreads, smem, s, p);
+    // large tiles hold two CTAs per SM (shared memory): twice the threads per
+    // CTA keep as many warps resident as four CTAs of small tiles
+    const int threads = nb >= 1024 ? kMpSmallThreadsMax : kMpThreads;
+    const int64_t blocks = std::min<int64_t>(p.m, mp_grid_cap((const void*)mp_small_kernel, threads, smem));
+    e = launch_dependent(mp_small_kernel, (unsigned)blocks, threads, smem, s, p);
     count_launch();
     return e;
 }
