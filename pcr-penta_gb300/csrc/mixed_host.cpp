@@ -394,15 +394,27 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
         for (const void* q : ptrs) if (reinterpret_cast<uintptr_t>(q) & 15) A.vec = 0;
     }
 
-    // Windows of the level-0 cyclic-reduction passes: whole systems when
-    // they fit one tile, else windows with a 2^(win+1) halo.
+    // Iterates: x_0 in X0 when more sweeps follow, every later x_s in the
+    // output (y, or Xout when y must keep the rhs for the report).
+    A.xout = keep_x ? A.Xout : y;
+    A.oss = keep_x ? n : ss;
+    A.ors = keep_x ? 1 : rs;
+
+    // Systems that fit one shared-memory tile: every sweep of a system in one
+    // CTA, the whole solve one launch (no sweep loop to drive)
+    if (pl.s1 == 0) {
+        if (out) *out = A;
+        const cudaError_t cs = launch_mp_small(A, st);
+        return cs == cudaSuccess ? PCRP_OK : cuda_error(cs, "mixed small-system launch");
+    }
+
+    // Windows of the level-0 cyclic-reduction passes (2^(win+1) halo), or
+    // block-PCR passes only (win = 0).
     SweepPlan S{};
     S.pl = pl; S.nb = nb; S.T = T;
-    S.windowed = pl.s1 > 0 && pl.win > 0;
-    S.cr_mode = pl.s1 == 0 || S.windowed;
-    if (pl.s1 == 0) {
-        S.W.nwin = 1; S.W.L = (int)nb; S.W.H = 0; S.W.K = 31; S.W.TRmax = (int)nb;
-    } else if (S.windowed) {
+    S.windowed = pl.win > 0;
+    S.cr_mode = S.windowed;
+    if (S.windowed) {
         S.W.H = 2 << pl.win; S.W.K = pl.win; S.W.L = kMpTryRows - 2 * S.W.H;
         S.W.nwin = cdiv(nb, S.W.L);
         S.W.TRmax = (int)std::min<int64_t>(S.W.L + 2 * S.W.H, nb);
@@ -412,22 +424,9 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     S.fused = max_sweeps >= 2 && S.cr_mode;
     A.first_fused = S.fused;
     A.cr_mode = S.cr_mode;
-    // Iterates: x_0 in X0 when more sweeps follow, every later x_s in the
-    // output (y, or Xout when y must keep the rhs for the report).
-    A.xout = keep_x ? A.Xout : y;
-    A.oss = keep_x ? n : ss;
-    A.ors = keep_x ? 1 : rs;
     S.P[0] = pl.s1 > 0 ? F(WL.P0) : nullptr;
     S.P[1] = pl.npass > 1 ? F(WL.P1) : nullptr;
     A.ctr = reinterpret_cast<int*>(base + WL.ctr);
-
-    // Systems that fit one shared-memory tile: every sweep of a system in one
-    // CTA, the whole solve one launch (no sweep loop to drive)
-    if (pl.s1 == 0) {
-        if (out) *out = A;
-        const cudaError_t cs = launch_mp_small(A, st);
-        return cs == cudaSuccess ? PCRP_OK : cuda_error(cs, "mixed small-system launch");
-    }
 
     cudaError_t ce;
     const int gm = keep_x ? 0 : graph_mode(st);
