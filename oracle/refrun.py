@@ -39,6 +39,9 @@ def lib():
         dp = ctypes.POINTER(ctypes.c_double)
         L.refrun_solve.argtypes = [ctypes.c_char_p, ctypes.c_int] + [dp] * 7 + [ctypes.c_int, ctypes.c_int]
         L.refrun_solve.restype = ctypes.c_int
+        L.refrun_time.argtypes = [ctypes.c_char_p, ctypes.c_int] + [dp] * 7 + [ctypes.c_int, ctypes.c_int,
+                                                                               ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+        L.refrun_time.restype = ctypes.c_int
         L.refrun_last_error.restype = ctypes.c_char_p
         _lib = L
     return _lib
@@ -55,3 +58,19 @@ def solve(arrs, m: int, n: int, variant: int, fma: bool = False) -> np.ndarray:
     if rc != 0:
         raise RuntimeError(f"refrun_solve rc={rc}: {L.refrun_last_error().decode()}")
     return x
+
+
+def time_solve(arrs, m: int, n: int, variant: int, fma: bool = False, reps: int = 3):
+    """Run the reference kernels once (returning x) and time `reps` more solves
+    on the GPU (CUDA events around the launches, inputs restored before each):
+    (x, mean milliseconds per solve)."""
+    L = lib()
+    dp = ctypes.POINTER(ctypes.c_double)
+    ins = [np.ascontiguousarray(v, dtype=np.float64) for v in arrs]
+    x = np.zeros(m * n, dtype=np.float64)
+    ms = ctypes.c_float(0.0)
+    rc = L.refrun_time(ptx_path(fma).encode(), variant, *[v.ctypes.data_as(dp) for v in ins],
+                       x.ctypes.data_as(dp), m, n, reps, ctypes.byref(ms))
+    if rc != 0:
+        raise RuntimeError(f"refrun_time rc={rc}: {L.refrun_last_error().decode()}")
+    return x, float(ms.value)
