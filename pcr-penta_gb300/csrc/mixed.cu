@@ -1338,8 +1338,11 @@ cudaError_t launch_mp_small(const MpArgs& p, cudaStream_t s)
                                          (int)mp_pass_smem(kMpMaxRows));
     if (e != cudaSuccess) return e;
     // large tiles hold two CTAs per SM (shared memory): twice the threads per
-    // CTA keep as many warps resident as four CTAs of small tiles
-    const int threads = nb >= 1024 ? kMpSmallThreadsMax : kMpThreads;
+    // CTA keep as many warps resident as four CTAs of small tiles; systems of
+    // fewer than 256 block rows get one thread per block row (whole warps),
+    // so small systems fill the SM with more CTAs instead of idle threads
+    const int threads = nb >= 1024 ? kMpSmallThreadsMax
+                        : nb >= kMpThreads ? kMpThreads : (int)std::max<int64_t>(32, (nb + 31) / 32 * 32);
     const int64_t blocks = std::min<int64_t>(p.m, mp_grid_cap((const void*)mp_small_kernel, threads, smem));
     e = launch_dependent(mp_small_kernel, (unsigned)blocks, threads, smem, s, p);
     count_launch();
