@@ -179,14 +179,15 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
     }
 
     // global passes: K strides each, windows of L rows plus 2*(2^K-1) halo rows.
-    // The s1 strides are spread evenly over the ceil(s1/fuse) passes (3+2+2,
-    // not 3+3+1: a one-stride pass spreads a pass's fixed costs over little
-    // work), and a pass of fewer strides turns the halo rows it does not need
-    // into tile rows.
+    // The s1 strides are spread evenly over the ceil(s1/fuse) passes, the
+    // longer passes last (2+2+3, not 3+3+1: a one-stride pass spreads a pass's
+    // fixed costs over little work, and the later passes' shorter subsystems
+    // fill their tiles better with the wider halo); a pass of fewer strides
+    // turns the halo rows it does not need into tile rows.
     const int npass = s1 > 0 ? (s1 + pl.fuse - 1) / pl.fuse : 0;
     int cur = 0;
     for (int ip = 0; ip < npass; ip++) {
-        const int K = s1 / npass + (ip < s1 % npass ? 1 : 0);
+        const int K = s1 / npass + (ip >= npass - s1 % npass ? 1 : 0);
         const int H = 2 * ((1 << K) - 1);
         const int Hfuse = 2 * ((1 << std::min(pl.fuse, s1)) - 1);
         int L = (pl.tile_rows > 0 ? pl.tile_rows : 1024) + 2 * (Hfuse - H);

@@ -66,14 +66,15 @@ __device__ inline int rg_plan(int64_t n, int cap, int fuse, int L0, int* K, int6
     const int ns = ref_strides(n);
     int s1 = 0;
     while (s1 < ns && cdiv64(n, int64_t(1) << s1) > cap) s1++;
-    // s1 strides spread evenly over ceil(s1/fuse) levels, as in the uniform
-    // planner; a level of fewer strides turns unneeded halo rows into tile rows
+    // s1 strides spread evenly over ceil(s1/fuse) levels, the longer ones
+    // last, as in the uniform planner; a level of fewer strides turns unneeded
+    // halo rows into tile rows
     const int npass = s1 > 0 ? (s1 + fuse - 1) / fuse : 0;
     const int hfuse = 2 * ((1 << min(fuse, max(s1, 1))) - 1);
     int P = 0, done = 0;
     int64_t g = 1;
     while (done < s1) {
-        const int k = s1 / npass + (P < s1 % npass ? 1 : 0);
+        const int k = s1 / npass + (P >= npass - s1 % npass ? 1 : 0);
         const int h = 2 * ((1 << k) - 1);
         int l = (L0 > 0 ? L0 : cap) + 2 * (hfuse - h);
         if (l + 2 * h > cap) l = cap - 2 * h;
