@@ -295,3 +295,25 @@ def test_mixed_interleaved_adapter_matches_contiguous(cuda, m, n):
     with pytest.raises(pcrp.PcrpError):
         run_mixed(inter, m, n, pcrp.INTERLEAVED, report=True,
                   opts=pcrp.Opts(workspace=ws.data_ptr(), workspace_bytes=small))
+
+
+@pytest.mark.parametrize("n", [700, 20000])
+def test_mixed_nan_input_reports_nonconvergence(cuda, n):
+    """A NaN in the right-hand side of one system poisons that system's norms:
+    the stopping rule never accepts it, the call ends after max_sweeps with
+    PCRP_ENOCONV (status 5), and the other systems are still solved (the
+    whole-system kernel for n = 700, the windowed passes for n = 20000)."""
+    import torch
+    m = 3
+    arrs = dd_bands(np.random.default_rng(11), m, n)
+    arrs[5][n + n // 2] = np.nan                       # system 1
+    t = to_device(arrs, "cuda:0")
+    with pytest.raises(pcrp.PcrpError) as ei:
+        pcrp.solve_mixed(*t, m, n, max_sweeps=4)
+    assert ei.value.status == 5
+    torch.cuda.synchronize()
+    x = t[5].cpu().numpy().reshape(m, n)
+    xg = np.asarray(O.ge(*arrs, m, n)).reshape(m, n)
+    for j in (0, 2):
+        assert np.abs(x[j] - xg[j]).max() / np.abs(xg[j]).max() <= TOL
+    assert np.isnan(x[1]).any()
