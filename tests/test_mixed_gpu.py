@@ -261,7 +261,7 @@ def test_mixed_inside_a_caller_graph_capture(cuda, mode):
         assert O.fwd_err(arrs[5].cpu().numpy(), O.ge(*host, m, n), m, n) <= TOL
 
 
-@pytest.mark.parametrize("m,n", [(5, 512), (3, 4096), (4, 65536), (2, 1000)])
+@pytest.mark.parametrize("m,n", [(5, 512), (3, 4096), (4, 65536), (2, 1000), (40, 1000), (40, 20), (33, 9000)])
 def test_mixed_interleaved_adapter_matches_contiguous(cuda, m, n):
     """An interleaved batch is solved through the layout adapter (transposed
     into contiguous copies, solved, transposed back): the same bits as the
@@ -284,14 +284,15 @@ def test_mixed_interleaved_adapter_matches_contiguous(cuda, m, n):
     pcrp.solve_mixed(None, *ti[1:4], None, ti[5], m, n, pcrp.INTERLEAVED, report=False)
     torch.cuda.synchronize()
     assert torch.equal(ti[5].view(n, m).t().contiguous().view(-1).view(torch.int64), tc[5].view(torch.int64))
-    # caller workspace: the interleaved size works, the contiguous one is refused
+    # caller workspace: the size the query gives for the interleaved layout
+    # works, a workspace that cannot hold the copies is refused
     need = pcrp.workspace_size(m, n, pcrp.INTERLEAVED, which=1)
     assert need > pcrp.workspace_size(m, n, pcrp.CONTIGUOUS, which=1)
     ws = torch.empty(need, dtype=torch.uint8, device="cuda")
     xw, _, _ = run_mixed(inter, m, n, pcrp.INTERLEAVED, report=True,
                          opts=pcrp.Opts(workspace=ws.data_ptr(), workspace_bytes=need))
     assert np.array_equal(np.ascontiguousarray(xw.reshape(n, m).T).ravel().view(np.uint64), xc.view(np.uint64))
-    small = pcrp.workspace_size(m, n, pcrp.CONTIGUOUS, which=1)
+    small = 6 * m * n * 8 - 1
     with pytest.raises(pcrp.PcrpError):
         run_mixed(inter, m, n, pcrp.INTERLEAVED, report=True,
                   opts=pcrp.Opts(workspace=ws.data_ptr(), workspace_bytes=small))
