@@ -94,7 +94,7 @@ cudaError_t launch_rpt(const PcrPassArgs& p, int threads, size_t smem, int64_t b
 
 }  // namespace
 
-int pcr_max_smem_rows() { return 2048; }   // 14 arrays * 2048 * 8 B = 224 KiB
+int pcr_max_smem_rows() { return 1920; }   // 15 arrays * 1920 * 8 B = 225 KiB
 
 size_t pcr_pass_smem_bytes(int TRmax) { return (size_t)TRmax * kSmemArrays * sizeof(double); }
 

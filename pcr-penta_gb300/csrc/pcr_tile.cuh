@@ -52,6 +52,20 @@ __device__ __forceinline__ double szero(unsigned s) { return __hiloint2double((i
 // x + z for a zero z with sign bit zs, x not NaN: x itself, unless x is a
 // zero too (then -0 only if both are -0: round-to-nearest)
 __device__ __forceinline__ double add_z(double x, unsigned zs) { return nz(x) ? x : szero(hiw(x) & zs); }
+// x / y from y's correctly rounded reciprocal r = RN(1/y) (__drcp_rn):
+// Markstein's correction (IBM J. Res. Dev. 1990): q0 = RN(x r) is within an
+// ulp of x/y, the remainder x - y q0 is exact in one FMA, and RN(q0 + rem r)
+// = RN(x / y) while no intermediate leaves the normal range, which the
+// exponent guard ensures; other operands take the division.
+__device__ __forceinline__ double mdiv(double x, double y, double r) {
+    const int ex = (int)((hiw(x) >> 20) & 0x7FFu), ey = (int)((hiw(y) >> 20) & 0x7FFu);
+    if ((unsigned)(ex - 100) <= 1846u && (unsigned)(ey - 100) <= 1846u && (unsigned)(ex - ey + 900) <= 1800u) {
+        const double q0 = __dmul_rn(x, r);
+        const double rem = __fma_rn(-y, q0, x);
+        return __fma_rn(rem, r, q0);
+    }
+    return dvd(x, y);
+}
 __device__ __forceinline__ bool finite4(double p, double q, double r, double s) {
     return max(max(hiw(p) & 0x7FF00000u, hiw(q) & 0x7FF00000u), max(hiw(r) & 0x7FF00000u, hiw(s) & 0x7FF00000u))
            < 0x7FF00000u;
@@ -64,7 +78,7 @@ __device__ __forceinline__ bool zero_state(double a, double b, double c, double 
 }
 
 constexpr int kMaxThreads = 256;
-constexpr int kSmemArrays = 14;   // 6 state + 6 T coefficients + 2 T multipliers
+constexpr int kSmemArrays = 15;   // 6 state + 6 T coefficients + 2 T multipliers + 1/cT
 
 // Global loads of the state; kL2Only reads through L2 only (ld.global.cg), for
 // persistent kernels that read data other CTAs wrote earlier in the same launch.
@@ -87,7 +101,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
     double* sd = sc + TRm;        double* se = sd + TRm;  double* sy = se + TRm;
     double* Ta = sy + TRm;        double* Tb = Ta + TRm;  double* Tc = Tb + TRm;
     double* Td = Tc + TRm;        double* Te = Td + TRm;  double* Tk = Te + TRm;
-    double* T1 = Tk + TRm;        double* T2 = T1 + TRm;
+    double* T1 = Tk + TRm;        double* T2 = T1 + TRm;  double* Tr = T2 + TRm;
 
     const int64_t sbase = p.offsets ? p.offsets[j] : j * p.src_ss;
     const int64_t dbase = p.offsets ? p.offsets[j] : j * p.dst_ss;
@@ -252,6 +266,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                     }
                     Ta[k] = aT; Tb[k] = bT; Tc[k] = cT; Td[k] = dT; Te[k] = eT; Tk[k] = kT;
                     T1[k] = al1; T2[k] = al2;
+                    Tr[k] = __drcp_rn(cT);
                 }
             }
         }
@@ -262,19 +277,19 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
         zrow = true; zdrow = true;
         // the reference's update of row i (kernel.cu:120-140, in place: phase
         // B reads no other row's state); folds the row's zero state into zrow
-        auto row_b = [&](int q, int k, bool hasL, bool hasR, double a1pre, double a2pre) {
+        auto row_b = [&](int q, int k, bool hasL, bool hasR, double a1pre, double a2pre, bool rcp) {
             const double ai = sa[k], bi = sb[k], ci = sc[k], di = sd[k], ei = se[k], yi = sy[k];
             double a1 = 0.0, b1 = 0.0, c1 = 0.0, d1 = 0.0, k1 = 0.0, f1 = a1pre;
             double b2 = 0.0, c2 = 0.0, d2 = 0.0, e2 = 0.0, k2 = 0.0, f2 = a2pre;
             if (hasL) {                    // kernel.cu:120-125
                 const double cTL = Tc[k - dl];
-                if (nz(cTL)) f1 = dvd(bi, cTL);
+                if (nz(cTL)) f1 = rcp ? mdiv(bi, cTL, Tr[k - dl]) : dvd(bi, cTL);
                 a1 = mul(f1, Ta[k - dl]); b1 = mul(f1, Tb[k - dl]); c1 = mul(f1, Td[k - dl]);
                 d1 = mul(f1, Te[k - dl]); k1 = mul(f1, Tk[k - dl]);
             }
             if (hasR) {                    // kernel.cu:127-132
                 const double cTR = Tc[k + dl];
-                if (nz(cTR)) f2 = dvd(di, cTR);
+                if (nz(cTR)) f2 = rcp ? mdiv(di, cTR, Tr[k + dl]) : dvd(di, cTR);
                 c2 = mul(f2, Tb[k + dl]); b2 = mul(f2, Ta[k + dl]); d2 = mul(f2, Td[k + dl]);
                 e2 = mul(f2, Te[k + dl]); k2 = mul(f2, Tk[k + dl]);
             }
@@ -331,7 +346,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                         const bool z = finite4(nb, nc, nd, ny);
                         zrow = zrow && z; zdrow = zdrow && z;
                     } else {
-                        row_b(q, k, hasL, hasR, a1pre, a2pre);
+                        row_b(q, k, hasL, hasR, a1pre, a2pre, false);
                     }
                 }
             }
@@ -375,7 +390,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                         const bool z = finite4(nb, nc, nd, ny);
                         zrow = zrow && z; zdrow = zdrow && z && !nz(nd);
                     } else {
-                        row_b(q, k, hasL, hasR, a1pre, a2pre);
+                        row_b(q, k, hasL, hasR, a1pre, a2pre, false);
                     }
                 }
             }
@@ -389,7 +404,7 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
                     // multipliers last assigned before Reduction-III (kernel.cu:96-112)
                     const double a1pre = hasR ? T1[k + dl] : ((t - 2 * dl >= 0) ? T1[k - dl] : al1p[q]);
                     const double a2pre = (t + 2 * dl <= nr - 1) ? T2[k + dl] : (hasL ? T2[k - dl] : al2p[q]);
-                    row_b(q, k, hasL, hasR, a1pre, a2pre);
+                    row_b(q, k, hasL, hasR, a1pre, a2pre, true);
                 }
             }
         }

@@ -27,7 +27,7 @@ from . import GEN_DOMINANT, Opts, generate_device, solve_f64, solve_mixed
 from .build import CSRC
 
 # (size-class upper bound n_max, batch m used to time it)
-F64_CLASSES = [(1024, 1024), (8192, 256), (131072, 64), (1 << 21, 8)]
+F64_CLASSES = [(512, 1024), (1024, 1024), (8192, 256), (131072, 64), (1 << 21, 8)]
 MP_CLASSES = [(1024, 2048), (8192, 1024), (131072, 128), (1 << 21, 16)]
 
 
@@ -55,7 +55,7 @@ def _batch(m, n, seed=1):
 
 
 def f64_candidates():
-    for smem, fuse, threads in itertools.product((512, 1024, 2048), (1, 2, 3, 4, 5), (128, 256)):
+    for smem, fuse, threads in itertools.product((480, 960, 1920), (1, 2, 3, 4, 5), (128, 256)):
         H = 2 * ((1 << fuse) - 1)
         if smem - 2 * H < 64:
             continue
