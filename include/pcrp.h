@@ -242,6 +242,17 @@ int64_t pcrp_kernel_launches(void);
  * reference. */
 pcrp_status pcrp_measure_fp64(double* dfma_per_s, double* ddiv_per_s, pcrp_stream stream);
 
+/* Checks the FP64 kernels' phase-B quotient (Markstein's correction from the
+ * correctly rounded reciprocal, inside its exponent guard) against IEEE
+ * division (__ddiv_rn) on `samples` seeded random operand pairs of class
+ * `mode` (0: exponents within 2^+-32, 1: the guard's whole range, 2: mantissas
+ * near all ones, 3: near powers of two, 4: any exponent, zeros, subnormals,
+ * inf and NaN included).  Synchronous.  *mismatches counts results whose bits
+ * differ (any NaN matches any NaN), *markstein the pairs inside the guard.  A
+ * diagnostic; no counterpart in the reference. */
+pcrp_status pcrp_check_quotients(int32_t mode, uint64_t seed, int64_t samples, uint64_t* mismatches,
+                                 uint64_t* markstein, pcrp_stream stream);
+
 /* ------------------------------------------------------------------------ */
 /* Seeded input generators (host memory, threads over systems)              */
 /* ------------------------------------------------------------------------ */

@@ -2,6 +2,7 @@
 // the FP64-pipe roofline of the bit-faithful path.
 #include <cuda_runtime.h>
 
+#include "pcr_tile.cuh"
 #include "pcrp_internal.h"
 
 namespace pcrp {
@@ -66,9 +67,92 @@ cudaError_t time_ms(Launch launch, cudaStream_t s, float* ms)
 }
 
 }  // namespace
+namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// A double of operand class `mode` from 64 random bits: 0 exponents within
+// 2^+-32, 1 every exponent the quotient's guard admits, 2 mantissas near all
+// ones, 3 mantissas near a power of two, 4 any finite or infinite exponent
+// (zeros, subnormals and the guard's excluded ranges included).
+__device__ __forceinline__ double operand(uint64_t r, int mode)
+{
+    uint64_t mant = r & 0xFFFFFFFFFFFFFull;
+    int e;
+    switch (mode) {
+    case 0: e = 1023 + (int)((r >> 52) % 64) - 32; break;
+    case 1: e = 100 + (int)((r >> 52) % 1847); break;
+    case 2: e = 1023 + (int)((r >> 52) % 16) - 8; mant |= 0xFFFFFFFFFFF00ull; break;
+    case 3: e = 1023 + (int)((r >> 52) % 16) - 8; mant &= 0xFFull; break;
+    default: e = (int)((r >> 52) % 2048); break;
+    }
+    return __longlong_as_double((long long)(((r >> 63) << 63) | ((uint64_t)e << 52) | mant));
+}
+
+// The phase-B quotient of the FP64 kernels (mdiv: Markstein's correction
+// from the correctly rounded reciprocal) against __ddiv_rn on random pairs.
+__global__ void __launch_bounds__(kProbeThreads)
+quotient_check(int mode, uint64_t seed, int64_t per_thread, unsigned long long* bad, unsigned long long* fast)
+{
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    unsigned long long nb = 0, nf = 0;
+    for (int64_t i = 0; i < per_thread; i++) {
+        const uint64_t r1 = mix64(seed ^ (t * 0x100000001B3ull + (uint64_t)i * 2));
+        const uint64_t r2 = mix64(seed + t * 0x9E37ull + (uint64_t)i * 2 + 1);
+        const double a = operand(r1, mode), b = operand(r2, (r2 & 1) ? 4 : mode);
+        if (!nz(b)) continue;                     // the kernels never divide by zero
+        const double q = mdiv(a, b, __drcp_rn(b)), ref = __ddiv_rn(a, b);
+        const bool same = __double_as_longlong(q) == __double_as_longlong(ref) || (q != q && ref != ref);
+        nb += !same;
+        const int ea = (int)((hiw(a) >> 20) & 0x7FFu), eb = (int)((hiw(b) >> 20) & 0x7FFu);
+        nf += (unsigned)(ea - 100) <= 1846u && (unsigned)(eb - 100) <= 1846u && (unsigned)(ea - eb + 900) <= 1800u;
+    }
+    atomicAdd(bad, nb);
+    atomicAdd(fast, nf);
+}
+
+}  // namespace
 }  // namespace pcrp
 
 using namespace pcrp;
+
+extern "C" pcrp_status pcrp_check_quotients(int32_t mode, uint64_t seed, int64_t samples, uint64_t* mismatches,
+                                            uint64_t* markstein, pcrp_stream stream)
+{
+    if (!mismatches || !markstein || samples < 0 || mode < 0 || mode > 4)
+        return set_error(PCRP_EINVAL, "pcrp_check_quotients: bad argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_error(e, "pcrp_check_quotients");
+    unsigned long long* cnt = nullptr;
+    e = cudaMallocAsync(reinterpret_cast<void**>(&cnt), 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return cuda_error(e, "pcrp_check_quotients allocation");
+    const unsigned grid = (unsigned)sms * 8;
+    const int64_t threads = (int64_t)grid * kProbeThreads;
+    const int64_t per = (samples + threads - 1) / threads;
+    unsigned long long host[2] = {0, 0};
+    e = cudaMemsetAsync(cnt, 0, sizeof host, s);
+    if (e == cudaSuccess) {
+        quotient_check<<<grid, kProbeThreads, 0, s>>>(mode, seed, per, cnt, cnt + 1);
+        count_launch();
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host, cnt, sizeof host, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(cnt, s);
+    if (e != cudaSuccess) return cuda_error(e, "pcrp_check_quotients");
+    *mismatches = host[0];
+    *markstein = host[1];
+    return PCRP_OK;
+}
 
 extern "C" pcrp_status pcrp_measure_fp64(double* dfma_per_s, double* ddiv_per_s, pcrp_stream stream)
 {

@@ -84,6 +84,7 @@ _SIGS = {
     "pcrp_version": [],
     "pcrp_kernel_launches": [],
     "pcrp_measure_fp64": [_vp, _vp, _vp],
+    "pcrp_check_quotients": [_i32, ctypes.c_uint64, _i64, _vp, _vp, _vp],
     "pcrp_generate": [_i32, ctypes.c_uint64, _i64, _i64, _i32] + [_vp] * 6 + [_i32],
     "pcrp_generate_device": [_i32, ctypes.c_uint64, _i64, _i64, _i32] + [_vp] * 6 + [_vp],
     "pcrp_ragged_sizes": [ctypes.c_uint64, _i64, _i64, _i64, _vp],
@@ -249,6 +250,16 @@ def measure_fp64(stream=None):
     f, d = ctypes.c_double(0.0), ctypes.c_double(0.0)
     _check(lib().pcrp_measure_fp64(ctypes.byref(f), ctypes.byref(d), _stream(stream)), "pcrp_measure_fp64")
     return f.value, d.value
+
+
+def check_quotients(mode: int, seed: int, samples: int, stream=None):
+    """(mismatches, pairs inside the guard) of the FP64 kernels' phase-B
+    quotient against IEEE division on `samples` random pairs of operand class
+    `mode` (pcrp_check_quotients); synchronous."""
+    bad, fast = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    _check(lib().pcrp_check_quotients(mode, seed, samples, ctypes.byref(bad), ctypes.byref(fast), _stream(stream)),
+           "pcrp_check_quotients")
+    return int(bad.value), int(fast.value)
 
 
 # ----------------------------------------------------------------------------

@@ -112,6 +112,16 @@ def test_zero_outer_bands_bitexact(cuda, n, path, opts, special, zero_d):
     assert_bitexact(x, ref, f"zero bands n={n} path={path} special={special} zero_d={zero_d}")
 
 
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4])
+def test_phase_b_quotients_match_ieee_division(cuda, mode):
+    """Phase B forms its two quotients from one correctly rounded reciprocal
+    of cT (Markstein's correction inside an exponent guard); on 2^28 random
+    pairs per operand class every quotient has the bits of __ddiv_rn."""
+    bad, fast = pcrp.check_quotients(mode, 1234 + mode, 1 << 28)
+    assert bad == 0
+    assert fast > (1 << 26)                       # the guard admits most pairs of every class
+
+
 def test_bands_are_not_modified(cuda):
     import torch
     for n in (300, 5000):
