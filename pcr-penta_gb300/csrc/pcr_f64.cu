@@ -24,8 +24,16 @@
 // same combination T(m) centred on m = i-d and m = i+d, built from identical
 // expressions (compare kernel.cu:77-79 with kernel.cu:103-105), so T(m) is
 // formed once per row in phase A and shared through shared memory in
-// phase B: 4 FP64 divisions per row and stride instead of the reference's 6,
-// with bit-identical results.  The reference's multiplier registers, which
+// phase B: 4 IEEE quotients per row and stride instead of the reference's 6,
+// with bit-identical results.  The two of phase B divide by cT of the
+// neighbours; phase A also stores cT's correctly rounded reciprocal
+// (__drcp_rn), and phase B finishes each quotient with Markstein's
+// correction (IBM J. Res. Dev. 34(1), 1990): q0 = RN(b r), the remainder
+// b - cT q0 exact in one FMA, RN(q0 + rem r) = RN(b / cT) when no
+// intermediate leaves the normal range, which an exponent guard ensures (other
+// operands take the division).  A reciprocal and two corrections cost ~10.5
+// DFMA slots against ~14.4 for two divisions; pcrp_check_quotients compares
+// them with IEEE division on random operand classes.  The reference's multiplier registers, which
 // outlive a stride and are reused when a Reduction-III pivot is exactly zero
 // (kernel.cu:122,129), are kept per row in registers inside a pass and in
 // two extra state arrays between passes.
