@@ -352,8 +352,9 @@ def run_ours(args, world, rank, local, pg):
                              "DFMA rate plus its IEEE divisions at the measured division rate "
                              "(pcrp_measure_fp64), over the solve's kernel time; the kernels form "
                              "operations with a zero operand (late strides, once a and e have "
-                             "underflowed) on the integer pipe, so frac is the rate of the reference's "
-                             "operations, not the FP64 pipe's busy share (ncu reports that)"}
+                             "underflowed) on the integer pipe and finish two quotients from one shared "
+                             "reciprocal, so frac is the rate of the reference's operations, not the "
+                             "FP64 pipe's busy share (ncu reports that)"}
 
     # the other precision on the same inputs: FP32 PCR + FP64 refinement when the
     # headline is plain FP64 (and the reverse), for the benchmark spec's ratio
