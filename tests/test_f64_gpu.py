@@ -122,6 +122,27 @@ def test_phase_b_quotients_match_ieee_division(cuda, mode):
     assert fast > (1 << 26)                       # the guard admits most pairs of every class
 
 
+@pytest.mark.parametrize("n", [700, 5000, 65536])
+def test_rows_scaled_across_the_exponent_range_bitexact(cuda, n):
+    """Rows scaled by random powers of two up to 2^+-500.  A power-of-two row
+    scale commutes exactly with every operation while nothing overflows, so
+    the solution keeps the unscaled system's bits; meanwhile numerators and
+    divisors of neighbouring rows differ by up to 2^1000, past the 900-octave
+    exponent guard of phase B's shared-reciprocal quotients, so the IEEE
+    division takes over for those pairs.  Bits equal the oracle's for both the
+    scaled and the unscaled system."""
+    rng = np.random.default_rng(n)
+    m = 4
+    arrs = dd_bands(rng, m, n)
+    scale = np.ldexp(1.0, rng.integers(-500, 501, m * n))
+    scaled = [v * scale for v in arrs]
+    x, _ = gpu_f64(scaled, m, n)
+    ref = O.pcr(*scaled, m, n)
+    assert np.isfinite(ref).all()
+    assert_bitexact(x, ref, f"scaled rows n={n}")
+    assert_bitexact(x, O.pcr(*arrs, m, n), f"scaled rows vs unscaled n={n}")
+
+
 def test_bands_are_not_modified(cuda):
     import torch
     for n in (300, 5000):
