@@ -95,6 +95,10 @@ typedef struct pcrp_mixed_info {
  * so the result is bit-identical to the reference kernels built with
  * -fmad=false.  Dispatches like the reference host code (main.cu:46-87):
  * n <= 1024 -> pcrp_solve_f64_small, otherwise pcrp_solve_f64_split.
+ * `a` and `e` may be NULL: that band is +0.0 and is not read; with both NULL
+ * (a tridiagonal batch) every stride runs the kernels' zero-operand form, with
+ * the bits of explicit +0.0 bands.  The same holds for the two paths below,
+ * pcrp_solve_f64_noalloc and pcrp_solve_host.
  * Replaces: main.cu:46-87 (time_* dispatch around pcr_penta and the splitting
  * kernels), kernel prototypes performanalysis.h:53-59. */
 pcrp_status pcrp_solve_f64(const double* a, const double* b, const double* c,
@@ -175,7 +179,8 @@ pcrp_status pcrp_residual_f64(const double* a, const double* b, const double* c,
                               int64_t m, int64_t n, int32_t layout, pcrp_stream stream);
 
 /* Solves a batch that lives in HOST memory: a..e and y are host arrays of
- * m*n doubles (page-locked memory lets the copies run asynchronously).  The
+ * m*n doubles (page-locked memory lets the copies run asynchronously; a
+ * NULL `a` or `e` is a zero band and is not copied).  The
  * systems are streamed through the GPU in chunks on two internal streams, so
  * the host<->device copies of one chunk overlap the solve of another; y
  * receives the solution.  precision 0 = pcrp_solve_f64 (bit-identical

@@ -148,10 +148,13 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
     if (force_small && n > 1024) return set_error(PCRP_EINVAL, "%s: n=%lld > 1024", who, (long long)n);
     if (force_split && n <= 1024 && n != 0) return set_error(PCRP_EINVAL, "%s: n=%lld <= 1024", who, (long long)n);
     if (m == 0 || n == 0) return PCRP_OK;
-    if (!a || !b || !c || !d || !e || !y) return set_error(PCRP_EINVAL, "%s: null array", who);
+    if (!b || !c || !d || !y) return set_error(PCRP_EINVAL, "%s: null array (only a and e may be null)", who);
     if (n > (int64_t(1) << 31) || m > (int64_t(1) << 40))
         return set_error(PCRP_EINVAL, "%s: size out of range", who);
 
+    // null a and e: a tridiagonal batch, both bands +0.0; the first pass
+    // reads neither, and every pass runs the zero-state strides
+    const bool tri = !a && !e;
     F64Plan pl = f64_plan(o, n);
     if (force_small && pl.smem_rows < n) pl.smem_rows = (int)n;         // the n <= 1024 path is one tile
     if (force_split && pl.smem_rows >= n) pl.smem_rows = 1024;         // the n > 1024 path splits
@@ -202,7 +205,7 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
         p.TRmax = (int)std::min<int64_t>(L + 2 * H, nrmax);
         for (int k = 0; k < NSTATE; k++) p.dst[k] = bufs[cur][k];
         p.dst_ss = n; p.dst_rs = 1;
-        cudaError_t ce = launch_pcr_pass(p, pl.threads, st);
+        cudaError_t ce = launch_pcr_pass(p, pl.threads, st, tri);
         if (ce != cudaSuccess) return cuda_error(ce, "pcr global pass launch");
         for (int k = 0; k < NSTATE; k++) p.src[k] = bufs[cur][k];
         p.src_ss = n; p.src_rs = 1;
@@ -216,7 +219,7 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
     p.TRmax = (int)nrmax;
     p.x = y; p.dst_ss = ss; p.dst_rs = rs;
     for (int k = 0; k < NSTATE; k++) p.dst[k] = nullptr;
-    cudaError_t ce = launch_pcr_pass(p, pl.threads, st);
+    cudaError_t ce = launch_pcr_pass(p, pl.threads, st, tri);
     if (ce != cudaSuccess) return cuda_error(ce, "pcr shared-memory pass launch");
     return PCRP_OK;
 }

@@ -79,7 +79,7 @@ extern "C" pcrp_status pcrp_solve_host(const double* a, const double* b, const d
         return set_error(PCRP_EINVAL, "%s: bad layout %d", who, layout);
     if (precision != 0 && precision != 1) return set_error(PCRP_EINVAL, "%s: precision %d (0 FP64, 1 mixed)", who, precision);
     if (m == 0 || n == 0) return PCRP_OK;
-    if (!a || !b || !c || !d || !e || !y) return set_error(PCRP_EINVAL, "%s: null array", who);
+    if (!b || !c || !d || !y) return set_error(PCRP_EINVAL, "%s: null array (only a and e may be null)", who);
     cudaStream_t st = (cudaStream_t)stream;
     int dev = 0;
     cudaError_t ce = cudaGetDevice(&dev);
@@ -113,8 +113,10 @@ extern "C" pcrp_status pcrp_solve_host(const double* a, const double* b, const d
         cudaStream_t s = S[q & 1];
         double* base = buf + (q & 1) * slot;
         double* dv[6];
-        for (int k = 0; k < 6; k++) dv[k] = base + (size_t)k * chunk * n;
-        for (int k = 0; k < 6 && ce == cudaSuccess; k++) ce = copy_chunk(dv[k], src[k], j0, mc, m, n, layout, true, s);
+        // a null band stays null on the device (a zero band, not copied)
+        for (int k = 0; k < 6; k++) dv[k] = src[k] ? base + (size_t)k * chunk * n : nullptr;
+        for (int k = 0; k < 6 && ce == cudaSuccess; k++)
+            if (src[k]) ce = copy_chunk(dv[k], src[k], j0, mc, m, n, layout, true, s);
         if (ce != cudaSuccess) return cuda_error(ce, "pcrp_solve_host: copy in");
         rc = precision == 0
                  ? f64_solve(dv[0], dv[1], dv[2], dv[3], dv[4], dv[5], mc, n, layout, &so, s, false, false, who)

@@ -90,13 +90,17 @@ cudaError_t launch_rz(const PcrPassArgs& p, int threads, size_t smem, int64_t bl
 // Passes whose longest stride reaches kZeroStride rows vote on the zero
 // state: the outer coefficients of diagonally dominant systems underflow at
 // strides ~2^8-2^10, and the vote (~10% of a dense stride) pays once two or
-// more strides of the pass run in that state.  Others keep the plain kernel.
+// more strides of the pass run in that state.  Others keep the plain kernel,
+// unless the batch is tridiagonal (a = e = 0 on entry): then every stride of
+// every pass is in that state and every pass votes.
 constexpr int64_t kZeroStride = 1024;
 
 template <int RPT>
-cudaError_t launch_rpt(const PcrPassArgs& p, int threads, size_t smem, int64_t blocks, cudaStream_t s)
+cudaError_t launch_rpt(const PcrPassArgs& p, bool tridiagonal, int threads, size_t smem, int64_t blocks,
+                       cudaStream_t s)
 {
-    if (p.K > 0 && (p.G << (p.K - 1)) >= kZeroStride) return launch_rz<RPT, true>(p, threads, smem, blocks, s);
+    if (tridiagonal || (p.K > 0 && (p.G << (p.K - 1)) >= kZeroStride))
+        return launch_rz<RPT, true>(p, threads, smem, blocks, s);
     return launch_rz<RPT, false>(p, threads, smem, blocks, s);
 }
 
@@ -106,7 +110,7 @@ int pcr_max_smem_rows() { return 1920; }   // 15 arrays * 1920 * 8 B = 225 KiB
 
 size_t pcr_pass_smem_bytes(int TRmax) { return (size_t)TRmax * kSmemArrays * sizeof(double); }
 
-cudaError_t launch_pcr_pass(const PcrPassArgs& p, int threads, cudaStream_t s)
+cudaError_t launch_pcr_pass(const PcrPassArgs& p, int threads, cudaStream_t s, bool tridiagonal)
 {
     if (threads <= 0 || threads > kMaxThreads) threads = kMaxThreads;
     threads = (threads + 31) / 32 * 32;
@@ -118,10 +122,10 @@ cudaError_t launch_pcr_pass(const PcrPassArgs& p, int threads, cudaStream_t s)
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     const size_t smem = pcr_pass_smem_bytes(p.TRmax);
-    if (rpt <= 1) return launch_rpt<1>(p, threads, smem, blocks, s);
-    if (rpt <= 2) return launch_rpt<2>(p, threads, smem, blocks, s);
-    if (rpt <= 4) return launch_rpt<4>(p, threads, smem, blocks, s);
-    return launch_rpt<8>(p, threads, smem, blocks, s);
+    if (rpt <= 1) return launch_rpt<1>(p, tridiagonal, threads, smem, blocks, s);
+    if (rpt <= 2) return launch_rpt<2>(p, tridiagonal, threads, smem, blocks, s);
+    if (rpt <= 4) return launch_rpt<4>(p, tridiagonal, threads, smem, blocks, s);
+    return launch_rpt<8>(p, tridiagonal, threads, smem, blocks, s);
 }
 
 }  // namespace pcrp

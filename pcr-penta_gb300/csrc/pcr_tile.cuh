@@ -119,11 +119,13 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
     const int64_t dstep = p.G * p.dst_rs;
     const int64_t soff = sbase + r * p.src_rs;              // local row 0
     const int64_t doff = dbase + r * p.dst_rs;
-    const double* __restrict__ ga = p.src[A_] + soff;
+    // a null outer band (a tridiagonal batch, first pass only) is +0.0
+    const bool has_a = p.src[A_] != nullptr, has_e = p.src[E_] != nullptr;
+    const double* __restrict__ ga = has_a ? p.src[A_] + soff : nullptr;
     const double* __restrict__ gb = p.src[B_] + soff;
     const double* __restrict__ gc = p.src[C_] + soff;
     const double* __restrict__ gd = p.src[D_] + soff;
-    const double* __restrict__ ge = p.src[E_] + soff;
+    const double* __restrict__ ge = has_e ? p.src[E_] + soff : nullptr;
     const double* __restrict__ gy = p.src[Y_] + soff;
 
     double al1p[RPT], al2p[RPT];
@@ -135,8 +137,10 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
         al1p[q] = 0.0; al2p[q] = 0.0;
         if (k < TR) {
             const int64_t gi = (t0 + k) * sstep;
-            const double a = gload<kL2Only>(ga + gi), b = gload<kL2Only>(gb + gi), c = gload<kL2Only>(gc + gi);
-            const double d = gload<kL2Only>(gd + gi), e = gload<kL2Only>(ge + gi), y = gload<kL2Only>(gy + gi);
+            const double a = has_a ? gload<kL2Only>(ga + gi) : 0.0;
+            const double e = has_e ? gload<kL2Only>(ge + gi) : 0.0;
+            const double b = gload<kL2Only>(gb + gi), c = gload<kL2Only>(gc + gi);
+            const double d = gload<kL2Only>(gd + gi), y = gload<kL2Only>(gy + gi);
             sa[k] = a; sb[k] = b; sc[k] = c; sd[k] = d; se[k] = e; sy[k] = y;
             if constexpr (kZero) {
                 const bool z = zero_state(a, b, c, d, e, y);

@@ -41,7 +41,7 @@ __host__ __device__ inline int ref_strides(int64_t n) {
 //   (offsets ? offsets[j] : j*ss) + (r + t*G) * rs
 // with (ss, rs) = (n, 1) for the contiguous layout and (1, m) interleaved.
 struct PcrPassArgs {
-    const double* src[NSTATE];   // state in (AL1_/AL2_ may be null: zeros)
+    const double* src[NSTATE];   // state in (A_/E_/AL1_/AL2_ may be null: zeros)
     double* dst[NSTATE];         // state out (non-final passes)
     double* x;                   // solution out (final pass)
     const int64_t* offsets;      // ragged first rows (nullable); ragged data is contiguous
@@ -58,8 +58,9 @@ struct PcrPassArgs {
     int TRmax;                   // shared-memory rows per CTA (>= L + 2H, or whole subsystem)
 };
 
-// Host-side launchers (pcr_f64.cu).
-cudaError_t launch_pcr_pass(const PcrPassArgs& p, int threads, cudaStream_t s);
+// Host-side launchers (pcr_f64.cu).  `tridiagonal`: the batch entered with
+// a = e = 0, so every pass compiles in the zero-state vote.
+cudaError_t launch_pcr_pass(const PcrPassArgs& p, int threads, cudaStream_t s, bool tridiagonal = false);
 // dst[k] (cols x rows) = transpose of src[k] (rows x cols), both row-major,
 // for up to 6 arrays in one launch; pairs with a null pointer are skipped
 // (layout.cu): interleaved n x m <-> contiguous m x n batches

@@ -189,7 +189,9 @@ def solve_mixed(a, b, c, d, e, y, m: int, n: int, layout: int = CONTIGUOUS, tol:
     return info
 
 
-def _host_ptr(x) -> int:
+def _host_ptr(x) -> Optional[int]:
+    if x is None:
+        return None
     if hasattr(x, "ctypes"):
         if not x.flags.c_contiguous:
             raise ValueError("expected a contiguous array")

@@ -143,6 +143,69 @@ def test_rows_scaled_across_the_exponent_range_bitexact(cuda, n):
     assert_bitexact(x, O.pcr(*arrs, m, n), f"scaled rows vs unscaled n={n}")
 
 
+def tridiagonal(rng, m, n, special=False):
+    """A diagonally dominant tridiagonal batch as five bands (a = e = +0.0);
+    `special` puts +-inf and NaN into a few systems."""
+    arrs = dd_bands(rng, m, n, garbage=True)
+    arrs[0][:] = 0.0
+    arrs[4][:] = 0.0
+    if special and m >= 3 and n >= 8:
+        arrs[2][n // 2] = np.inf
+        arrs[5][n + n // 3] = np.nan
+        arrs[1][2 * n + n // 4] = -np.inf
+    return arrs
+
+
+def solve_null_outer(arrs, m, n, layout, drop=(0, 4), path="auto", opts=None):
+    """pcrp_solve_f64 with the bands at `drop` passed as NULL."""
+    import torch
+    t = to_device(arrs, "cuda:0")
+    args = [None if k in drop else v for k, v in enumerate(t)]
+    pcrp.solve_f64(*args, m, n, layout, opts=opts, path=path)
+    torch.cuda.synchronize()
+    return t[5].cpu().numpy()
+
+
+@pytest.mark.parametrize("n,path,opts", [
+    (1, "small", None), (300, "small", None), (1024, "auto", None), (1025, "split", None),
+    (5000, "auto", None), (65536, "auto", None), (70001, "auto", None),
+    (3000, "split", dict(smem_rows=16, fuse_strides=5, tile_rows=300, threads=64)),
+])
+@pytest.mark.parametrize("layout", [pcrp.CONTIGUOUS, pcrp.INTERLEAVED])
+@pytest.mark.parametrize("special", [False, True])
+def test_tridiagonal_null_outer_bands_bitexact(cuda, n, path, opts, layout, special):
+    """a = e = NULL, a tridiagonal batch: the bands are +0.0 and not read, and
+    every pass runs the zero-operand strides (the vote still checks every
+    tile, so non-finite systems take the FP64 operations).  Bits equal the
+    oracle's on explicit +0.0 bands and the solve given those bands."""
+    m = 3
+    arrs = to_layout(tridiagonal(np.random.default_rng(7 * n + special), m, n, special), m, n, layout)
+    o = pcrp.Opts(**opts) if opts else None
+    x = solve_null_outer(arrs, m, n, layout, path=path, opts=o)
+    assert_bitexact(x, O.pcr(*arrs, m, n, layout), f"tridiagonal n={n} layout={layout}")
+    xz, _ = gpu_f64(arrs, m, n, layout, path=path, opts=o)
+    assert_bitexact(x, xz, f"tridiagonal NULL vs +0.0 bands n={n}")
+
+
+@pytest.mark.parametrize("n", [700, 9000])
+@pytest.mark.parametrize("drop", [(0,), (4,)])
+def test_one_null_outer_band_bitexact(cuda, n, drop):
+    """Only a (or only e) NULL: that band is +0.0, the other is read."""
+    m = 4
+    arrs = dd_bands(np.random.default_rng(n + drop[0]), m, n)
+    arrs[drop[0]][:] = 0.0
+    x = solve_null_outer(arrs, m, n, pcrp.CONTIGUOUS, drop=drop)
+    assert_bitexact(x, O.pcr(*arrs, m, n), f"band {drop} NULL n={n}")
+
+
+def test_null_inner_band_is_refused(cuda):
+    L = pcrp.lib()
+    t = to_device(dd_bands(np.random.default_rng(0), 2, 100), "cuda:0")
+    p = [v.data_ptr() for v in t]
+    rc = L.pcrp_solve_f64(p[0], None, p[2], p[3], p[4], p[5], 2, 100, 0, None, None)
+    assert rc == 1 and "only a and e may be null" in pcrp.last_error()   # PCRP_EINVAL
+
+
 def test_bands_are_not_modified(cuda):
     import torch
     for n in (300, 5000):

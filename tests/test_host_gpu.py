@@ -24,6 +24,28 @@ def test_host_f64_equals_device(cuda, m, n, layout):
         assert np.array_equal(u.numpy(), v)
 
 
+@pytest.mark.parametrize("layout", [0, 1])
+def test_host_tridiagonal_null_outer_bands(cuda, layout):
+    """NULL a and e through the host entry point: not copied, same bits as
+    explicit +0.0 bands on the device."""
+    import torch
+    m, n = 10, 3000
+    arrs = dd_bands(np.random.default_rng(5), m, n)
+    arrs[0][:] = 0.0
+    arrs[4][:] = 0.0
+    arrs = to_layout(arrs, m, n, layout)
+    xd, _ = gpu_f64(arrs, m, n, layout)
+    h = [None if k in (0, 4) else torch.from_numpy(v.copy()).pin_memory() for k, v in enumerate(arrs)]
+    pcrp.solve_host(*h, m, n, layout, precision=0)
+    torch.cuda.synchronize()
+    assert_bitexact(h[5].numpy(), xd, f"host tridiagonal layout={layout}")
+    hm = [None if k in (0, 4) else v.copy() for k, v in enumerate(arrs)]
+    pcrp.solve_host(*hm, m, n, layout, precision=1)
+    torch.cuda.synchronize()
+    xr = O.ge(*arrs, m, n, layout)
+    assert O.fwd_err(hm[5], xr, m, n, layout) <= 1e-12
+
+
 def test_host_mixed_meets_tolerance_pageable(cuda):
     import torch
     m, n = 11, 3000

@@ -28,6 +28,20 @@ def test_noalloc_matches_solve_f64_twice(cuda):
         assert_bitexact(got[5].cpu().numpy(), ref[5].cpu().numpy(), f"noalloc call {k}")
 
 
+def test_noalloc_tridiagonal_null_outer_bands(cuda):
+    import torch
+    m, n = 4, 65536
+    arrs = dd_bands(np.random.default_rng(9), m, n)
+    arrs[0][:] = 0.0
+    arrs[4][:] = 0.0
+    ref = to_device(arrs, cuda)
+    pcrp.solve_f64(*ref, m, n)
+    got = to_device(arrs, cuda)
+    pcrp.solve_f64_noalloc(None, got[1], got[2], got[3], None, got[5], m, n)
+    torch.cuda.synchronize()
+    assert_bitexact(got[5].cpu().numpy(), ref[5].cpu().numpy(), "noalloc tridiagonal")
+
+
 def test_noalloc_refuses_batches_beyond_its_scratch(cuda):
     L = pcrp.lib()
     rc = L.pcrp_solve_f64_noalloc(1, 1, 1, 1, 1, 1, 16, 65536, 0, None)
