@@ -357,9 +357,11 @@ size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_s
 // kernel arguments (per-system status arrays live in the workspace).
 pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, const double* d, const double* e,
                           double* y, int64_t m, int64_t n, int64_t ss, int64_t rs, double tol, int max_sweeps,
-                          const pcrp_opts* opts, bool keep_x, void* ws, cudaStream_t st, MpArgs* out)
+                          const pcrp_opts* opts, bool keep_x, void* ws, cudaStream_t st, MpArgs* out,
+                          const MixedDest* dest, bool* dest_written)
 {
     const char* who = "pcrp_solve_mixed";
+    if (dest_written) *dest_written = false;
     const int64_t nb = (n + 1) / 2, T = m * nb;
     const MpPlan pl = mp_plan(nb, opts);
     if (pl.npass > kMpMaxPasses) return set_error(PCRP_EINVAL, "%s: n too large for the pass plan", who);
@@ -403,6 +405,10 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     // Systems that fit one shared-memory tile: every sweep of a system in one
     // CTA, the whole solve one launch (no sweep loop to drive)
     if (pl.s1 == 0) {
+        if (dest && !keep_x) {
+            A.xout = dest->x; A.oss = dest->ss; A.ors = dest->rs;
+            if (dest_written) *dest_written = true;
+        }
         if (out) *out = A;
         const cudaError_t cs = launch_mp_small(A, st);
         return cs == cudaSuccess ? PCRP_OK : cuda_error(cs, "mixed small-system launch");
@@ -508,10 +514,14 @@ extern "C" pcrp_status pcrp_solve_mixed(const double* a, const double* b, const 
     }
     double* ys = adapt ? cpy[5] : y;             // the solver's y: the copy, or y itself
     MpArgs A{};
-    rc = mixed_enqueue(a, b, c, d, e, ys, m, n, ss, rs, tol, max_sweeps, opts, info != nullptr, ws, st, &A);
+    // whole systems scatter x into the interleaved y from their final copy
+    const MixedDest yd{y, 1, m};
+    bool y_written = false;
+    rc = mixed_enqueue(a, b, c, d, e, ys, m, n, ss, rs, tol, max_sweeps, opts, info != nullptr, ws, st, &A,
+                       adapt ? &yd : nullptr, &y_written);
     if (rc != PCRP_OK) return rc;
     auto adapt_out = [&]() -> pcrp_status {
-        if (!adapt) return PCRP_OK;
+        if (!adapt || y_written) return PCRP_OK;
         const double* from[1] = {ys};
         double* to[1] = {y};
         cudaError_t te = launch_transpose(from, to, 1, m, n, st);

@@ -3,6 +3,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "pcrp.h"
+
 namespace pcrp {
 
 constexpr int kMpTile = 512;       // rows per CTA of the refinement kernel (2 per thread)
@@ -115,6 +117,23 @@ struct MpWindows {
     int64_t nwin;                       // windows per system
     int L, H, K, TRmax;                 // core rows, halo rows each side, levels (31: whole system), tile rows
 };
+
+// Where a solve that runs as one whole-system launch writes x when that is
+// not its y (the caller's interleaved y behind the layout adapter): the
+// kernel's final copy scatters x there, which takes the place of the
+// transpose back.
+struct MixedDest {
+    double* x;
+    int64_t ss, rs;                     // system / row strides of x
+};
+
+// Enqueues a uniform batch on `st` (mixed_host.cpp).  With `dest`, a solve of
+// whole systems that keeps no report writes x to *dest and sets
+// *dest_written; any other solve ignores it.
+pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, const double* d, const double* e,
+                          double* y, int64_t m, int64_t n, int64_t ss, int64_t rs, double tol, int max_sweeps,
+                          const pcrp_opts* opts, bool keep_x, void* ws, cudaStream_t st, MpArgs* out,
+                          const MixedDest* dest = nullptr, bool* dest_written = nullptr);
 
 cudaError_t launch_mp_init(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_first(const MpArgs& p, const MpWindows& g, cudaStream_t s);

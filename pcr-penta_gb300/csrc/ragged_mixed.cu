@@ -23,9 +23,6 @@ namespace pcrp {
 
 pcrp_status get_workspace(const pcrp_opts* o, size_t bytes, cudaStream_t s, void** out);
 size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_sweeps, bool info, int32_t layout);
-pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, const double* d, const double* e,
-                          double* y, int64_t m, int64_t n, int64_t ss, int64_t rs, double tol, int max_sweeps,
-                          const pcrp_opts* opts, bool keep_x, void* ws, cudaStream_t st, MpArgs* out);
 
 namespace {
 
