@@ -10,7 +10,7 @@ resident in HBM.  Prints ONE JSON line (rank 0).
 
 Metric: Gunknowns/s = (systems x rows, all ranks) / device time per step.
 A step solves the whole batch once; it first restores the right-hand side
-with one device copy (8 B/unknown, counted in `traffic_note`) because the
+with one device copy (16 B/unknown, named in `roofline.traffic_note`) because the
 solve overwrites y.  The inputs (0.8 GB at m=256, n=65536) exceed the 129 MB
 L2, so no L2 flush is needed between steps.
 
@@ -35,6 +35,22 @@ sys.path.insert(0, os.path.join(ROOT, "pcr-penta_gb300"))
 METRIC = "Gunknowns/s, % of 8 TB/s HBM; FP32+IR vs FP64 PCR at ≤1e-12 fwd err"
 UNIT = "Gunknowns/s"
 BYTES_PER_UNKNOWN = 56          # 5 FP64 bands + FP64 rhs read once, FP64 x written once
+
+# DRAM bytes per unknown of one solve (dram__bytes_read.sum +
+# dram__bytes_write.sum over the solve's launches) from ncu captures of a
+# smaller batch of the same systems (inputs still larger than L2), scaled to
+# the bench's batch by unknowns: systems are independent, so the traffic per
+# unknown does not depend on m.  Keyed by (config, solver); used only for the
+# config's own layout and the autotuned plan.  The capture commands are in the
+# profiles named here.
+MEASURED_TRAFFIC = {
+    ("c1", "f64"): (517.0, "ncu capture m=48 n=65536, the 5 pcr_pass_kernel launches of one solve "
+                           "(profiles/pcr_pass_kernel_f64_m256_n65536.md)"),
+    ("c1", "mixed"): (133.2, "ncu capture m=48 n=65536, mp_first_kernel + mp_try_kernel of one solve "
+                             "(profiles/mixed_kernels_m256_n65536.md)"),
+    ("c2", "mixed"): (123.0, "ncu capture m=1024 n=4096, the mp_small_kernel launch of one solve "
+                             "(profiles/mixed_small_kernel_c2_m4096_n4096.md)"),
+}
 
 
 def ref_strides(n: int) -> int:
@@ -487,6 +503,15 @@ def run_ours(args, world, rank, local, pg):
 
     if rank != 0:
         return
+    # measured DRAM traffic of one solve (bytes), where a capture exists
+    mt = MEASURED_TRAFFIC.get((args.config, args.solver))
+    if mt is not None and not args.opts and "layout" not in cfg:
+        traffic = mt[0] * m * n
+        traffic_note = (f"bytes per solve: {mt[0]} B/unknown x {m * n} unknowns, {mt[1]}; "
+                        f"each timed step also restores y (one device copy, 16 B/unknown of traffic)")
+    else:
+        traffic = None
+        traffic_note = "no ncu capture of this workload; each timed step also restores y (one device copy)"
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -504,7 +529,8 @@ def run_ours(args, world, rank, local, pg):
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 6 * 8 * m * n,
                 "d2h_bytes_per_step": 8 * m * n, "ms_per_step": e_ms},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None,
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "traffic_note": traffic_note,
                      "note": f"algorithmic {BYTES_PER_UNKNOWN} B/unknown over the solve's kernel time "
                              f"({kms_med:.3f} ms); peak {peak_kind}"},
         "clocks": clk.summary(),

@@ -58,3 +58,40 @@ def test_fp64_ops_matches_row_walk(n):
 
 def test_ref_strides():
     assert [bench.ref_strides(n) for n in (1, 2, 3, 4, 5, 8, 9, 1000, 1024, 1025)] == [0, 1, 1, 2, 2, 3, 3, 9, 10, 10]
+
+
+def dram_mb(path, names):
+    """Sum of the MB figures on the profile table rows whose first cell is
+    one of `names` (every column of the row)."""
+    tot = 0.0
+    with open(path) as f:
+        for line in f:
+            cells = [c.strip() for c in line.strip().strip("|").split("|")]
+            if cells and cells[0] in names:
+                for c in cells[1:]:
+                    for v in c.split("/"):
+                        v = v.strip()
+                        if v.replace(".", "", 1).isdigit():
+                            tot += float(v)
+    return tot
+
+
+@pytest.mark.parametrize("key,col_names,units", [
+    (("c1", "f64"), ["dram__bytes_read.sum (MB)", "dram__bytes_write.sum (MB)"], 48 * 65536),
+    (("c1", "mixed"), ["dram__bytes_read.sum (MB)", "dram__bytes_write.sum (MB)"], 48 * 65536),
+])
+def test_measured_traffic_matches_profiles(key, col_names, units):
+    """The bench's DRAM bytes per unknown equal the committed captures' sums."""
+    per, note = bench.MEASURED_TRAFFIC[key]
+    prof = os.path.join(bench.ROOT, note.split("(")[-1].rstrip(")"))
+    got = dram_mb(prof, col_names) * 1e6 / units
+    assert abs(got - per) < 0.5, (got, per)
+
+
+def test_measured_traffic_c2_matches_profile():
+    per, note = bench.MEASURED_TRAFFIC[("c2", "mixed")]
+    prof = os.path.join(bench.ROOT, note.split("(")[-1].rstrip(")"))
+    with open(prof) as f:
+        row = next(line for line in f if line.startswith("| dram__bytes_read / write (MB)"))
+    rd, wr = [float(v) for v in row.split("|")[2].split("/")]   # the current kernel's column
+    assert abs((rd + wr) * 1e6 / (1024 * 4096) - per) < 0.5
