@@ -202,6 +202,7 @@ pcrp_status pcrp_solve_host(const double* a, const double* b, const double* c,
 /* Solves nsys systems of uneven size in one persistent kernel.  System k
  * occupies rows offsets[k] .. offsets[k+1]-1 of the six arrays (contiguous);
  * `offsets` is a DEVICE array of nsys+1 int64 values with offsets[0] = 0.
+ * `a` and `e` may be NULL (zero bands, not read).
  * A device-side work queue bins the systems: those of at most
  * opts->smem_rows rows are solved whole in shared memory, larger ones are
  * split by global-memory stride passes first.  mode 0 = FP64 PCR-Penta

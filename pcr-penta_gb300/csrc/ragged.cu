@@ -368,7 +368,8 @@ extern "C" pcrp_status pcrp_solve_ragged(const double* a, const double* b, const
     if (nsys < 0 || max_rows < 0) return set_error(PCRP_EINVAL, "pcrp_solve_ragged: negative size");
     if (mode != 0 && mode != 1) return set_error(PCRP_EINVAL, "pcrp_solve_ragged: mode %d (0 FP64, 1 mixed)", mode);
     if (nsys == 0 || max_rows == 0) return PCRP_OK;
-    if (!offsets || !a || !b || !c || !d || !e || !y) return set_error(PCRP_EINVAL, "pcrp_solve_ragged: null pointer");
+    if (!offsets || !b || !c || !d || !y)
+        return set_error(PCRP_EINVAL, "pcrp_solve_ragged: null pointer (only a and e may be null)");
     if (nsys > (int64_t(1) << 24) || max_rows > (int64_t(1) << 31))
         return set_error(PCRP_EINVAL, "pcrp_solve_ragged: size out of range");
     if (mode == 0) return ragged_f64(a, b, c, d, e, y, offsets, nsys, max_rows, opts, (cudaStream_t)stream);

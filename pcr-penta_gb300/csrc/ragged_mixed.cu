@@ -40,11 +40,11 @@ __global__ void rgm_gather_kernel(const double* __restrict__ a, const double* __
         const int64_t k = sys[s];
         const int64_t o = offsets[k], n = offsets[k + 1] - o;
         if (i < n) {
-            pa[q] = i >= 2 ? a[o + i] : 0.0;
+            pa[q] = (a && i >= 2) ? a[o + i] : 0.0;             // a null outer band is zero
             pb[q] = i >= 1 ? b[o + i] : 0.0;
             pc[q] = c[o + i];
             pd[q] = i + 1 < n ? d[o + i] : 0.0;
-            pe[q] = i + 2 < n ? e[o + i] : 0.0;
+            pe[q] = (e && i + 2 < n) ? e[o + i] : 0.0;
             py[q] = y[o + i];
         } else {
             pa[q] = 0.0; pb[q] = 0.0; pc[q] = 1.0; pd[q] = 0.0; pe[q] = 0.0; py[q] = 0.0;

@@ -57,6 +57,29 @@ def test_ragged_f64_log_uniform_sizes_match_uniform_path(cuda):
         assert_bitexact(x1[sl], t[5].cpu().numpy(), f"system {k} n={sizes[k]}")
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+def test_ragged_tridiagonal_null_outer_bands(cuda, mode):
+    """a = e = NULL: FP64 mode gives the oracle's bits on explicit +0.0 bands,
+    mixed mode meets the 1e-12 bar against elimination."""
+    import torch
+    arrs, offs = ragged_batch(SIZES, 11)
+    arrs[0][:] = 0.0
+    arrs[4][:] = 0.0
+    t = [None if k in (0, 4) else torch.from_numpy(v).to(cuda) for k, v in enumerate(arrs)]
+    o = torch.from_numpy(offs).to(cuda)
+    sizes = np.diff(offs)
+    pcrp.solve_ragged(*t, o, len(sizes), int(sizes.max()), mode=mode)
+    torch.cuda.synchronize()
+    x = t[5].cpu().numpy()
+    if mode == 0:
+        assert_bitexact(x, O.ragged(*arrs, offs[:-1], sizes, kind="pcr"), "ragged tridiagonal f64")
+    else:
+        xr = O.ragged(*arrs, offs[:-1], sizes, kind="ge")
+        for k in range(len(sizes)):
+            sl = slice(offs[k], offs[k + 1])
+            assert O.fwd_err(x[sl], xr[sl], 1, int(sizes[k])) <= 1e-12, f"system {k}"
+
+
 def test_ragged_rejects_bad_offsets(cuda):
     import torch
     arrs, offs = ragged_batch([5, 6], 2)
