@@ -186,8 +186,9 @@ pcrp_status pcrp_residual_f64(const double* a, const double* b, const double* c,
  * receives the solution.  precision 0 = pcrp_solve_f64 (bit-identical
  * results), 1 = pcrp_solve_mixed (tol, max_sweeps as there; no report).
  * Asynchronous on `stream`: the host arrays must stay valid until the stream
- * reaches the end of the call.  opts->workspace, if given, holds the staging
- * chunks (two chunks of 6 arrays).  No counterpart in the reference (its host
+ * reaches the end of the call.  Chunks grow from ceil(m/32) systems threefold
+ * up to ceil(m/4) (at most 2^26 unknowns).  opts->workspace, if given, holds
+ * the staging chunks: 2 x 6 x (largest chunk) x n doubles.  No counterpart in the reference (its host
  * code never moves data; this is the path of a caller whose batch is on the host). */
 pcrp_status pcrp_solve_host(const double* a, const double* b, const double* c,
                             const double* d, const double* e, double* y,

@@ -4,7 +4,11 @@
 //
 // Two internal streams per device alternate over the chunks: chunk c is
 // copied in, solved and copied out on stream c % 2, so while one stream runs
-// its solve the copy engines serve the other.  The caller's stream is joined
+// its solve the copy engines serve the other.  Chunks grow: the first holds
+// ceil(m/32) systems, so little copying precedes the first solve, and each
+// next one three times as many, up to ceil(m/4), because a solve of few
+// systems fills the GPU less well than a large one (measured on GB300, m=256
+// n=65536: 0.102 ms per system at m=8, 0.088 at 32, 0.084 at 64).  The caller's stream is joined
 // at both ends with events, so the call is asynchronous like the device
 // entry points (the host arrays must stay valid until the stream reaches
 // that point; page-locked host memory lets the copies run asynchronously).
@@ -89,10 +93,11 @@ extern "C" pcrp_status pcrp_solve_host(const double* a, const double* b, const d
     pcrp_status rc = dev_streams(dev, S, E);
     if (rc != PCRP_OK) return rc;
 
-    // chunks: about 8 per call, at most 2^26 unknowns each
-    int64_t chunk = std::max<int64_t>(1, (m + 7) / 8);
+    // chunk sizes: ceil(m/32) systems, then x3 per chunk up to ceil(m/4);
+    // at most 2^26 unknowns each
+    int64_t chunk = std::max<int64_t>(1, (m + 3) / 4);
     while (chunk > 1 && chunk * n > (int64_t(1) << 26)) chunk = (chunk + 1) / 2;
-    const int64_t nchunks = (m + chunk - 1) / chunk;
+    const int64_t first = std::min(chunk, std::max<int64_t>(1, (m + 31) / 32));
     const size_t slot = (size_t)6 * chunk * n;
     void* ws = nullptr;
     rc = get_workspace(opts, 2 * slot * sizeof(double), st, &ws);
@@ -108,8 +113,9 @@ extern "C" pcrp_status pcrp_solve_host(const double* a, const double* b, const d
     ce = cudaEventRecord(E[0], st);
     for (int k = 0; k < 2 && ce == cudaSuccess; k++) ce = cudaStreamWaitEvent(S[k], E[0], 0);
     if (ce != cudaSuccess) return cuda_error(ce, "pcrp_solve_host: stream join");
-    for (int64_t q = 0; q < nchunks; q++) {
-        const int64_t j0 = q * chunk, mc = std::min(chunk, m - j0);
+    int64_t j0 = 0, next = first;
+    for (int64_t q = 0; j0 < m; q++, j0 += next, next = std::min(3 * next, chunk)) {
+        const int64_t mc = std::min(next, m - j0);
         cudaStream_t s = S[q & 1];
         double* base = buf + (q & 1) * slot;
         double* dv[6];
