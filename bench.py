@@ -373,7 +373,7 @@ def run_ours(args, world, rank, local, pg):
                              "FP64 pipe's busy share (ncu reports that)"}
 
     # the other precision on the same inputs: FP32 PCR + FP64 refinement when the
-    # headline is plain FP64 (and the reverse), for the benchmark spec's ratio
+    # headline is plain FP64 (and the reverse), for the mixed/FP64 speed ratio
     other = None
     if args.compare:
         other_solver = "mixed" if args.solver == "f64" else "f64"
@@ -586,7 +586,8 @@ def run_ours(args, world, rank, local, pg):
 
 
 def run_ragged_bench(args, world, rank, local, pg):
-    """configs[3]: ragged batch through pcrp_solve_ragged (FP64 and mixed) against
+    """Ragged batch (4096 systems, log-uniform sizes 32..65536) through
+    pcrp_solve_ragged (FP64 and mixed) against
     the per-size sequence of launches (one pcrp_solve_f64 call per system)."""
     import numpy as np
     import torch

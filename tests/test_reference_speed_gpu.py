@@ -14,7 +14,7 @@ R = pytest.importorskip("refrun")
 
 pytestmark = pytest.mark.gpu
 
-CASES = [  # (workload, m, n, reference variant): configs[0] and configs[1] sizes
+CASES = [  # (workload, m, n, reference variant): the shared-memory and the large-n workloads
     ("n=512 (shared-memory path)", 1024, 512, 0),
     ("n=65536, global_cached_shared_tile_splitting + 2nd stage", 256, 65536, 2),
     ("n=65536, global_cached_global_tile_splitting + 2nd stage", 256, 65536, 3),
