@@ -205,10 +205,11 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
         p.TRmax = (int)std::min<int64_t>(L + 2 * H, nrmax);
         for (int k = 0; k < NSTATE; k++) p.dst[k] = bufs[cur][k];
         p.dst_ss = n; p.dst_rs = 1;
+        p.dst_sub = 1;                      // the next pass reads each subsystem in one run
         cudaError_t ce = launch_pcr_pass(p, pl.threads, st, tri);
         if (ce != cudaSuccess) return cuda_error(ce, "pcr global pass launch");
         for (int k = 0; k < NSTATE; k++) p.src[k] = bufs[cur][k];
-        p.src_ss = n; p.src_rs = 1;
+        p.src_ss = n; p.src_rs = 1; p.src_sub = 1;
         cur ^= 1;
         p.G <<= K;
     }
@@ -217,7 +218,7 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
     const int64_t nrmax = ceil_div(n, p.G);
     p.K = ns - s1; p.H = 0; p.L = (int)nrmax; p.final_step = 1; p.nwin = 1;
     p.TRmax = (int)nrmax;
-    p.x = y; p.dst_ss = ss; p.dst_rs = rs;
+    p.x = y; p.dst_ss = ss; p.dst_rs = rs; p.dst_sub = 0;
     for (int k = 0; k < NSTATE; k++) p.dst[k] = nullptr;
     cudaError_t ce = launch_pcr_pass(p, pl.threads, st, tri);
     if (ce != cudaSuccess) return cuda_error(ce, "pcr shared-memory pass launch");

@@ -115,9 +115,10 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
     const int64_t t1  = min(whi + (int64_t)p.H, nr);
     const int TR = (int)(t1 - t0);
     const int tid = threadIdx.x, bd = blockDim.x;
-    const int64_t sstep = p.G * p.src_rs;                   // distance of local rows t, t+1
+    // distance of local rows t, t+1 and local row 0 of the source
+    const int64_t sstep = p.src_sub ? 1 : p.G * p.src_rs;
+    const int64_t soff = p.src_sub ? sbase + r * (nsys / p.G) + min(r, nsys % p.G) : sbase + r * p.src_rs;
     const int64_t dstep = p.G * p.dst_rs;
-    const int64_t soff = sbase + r * p.src_rs;              // local row 0
     const int64_t doff = dbase + r * p.dst_rs;
     // a null outer band (a tridiagonal batch, first pass only) is +0.0
     const bool has_a = p.src[A_] != nullptr, has_e = p.src[E_] != nullptr;
@@ -435,12 +436,22 @@ __device__ __forceinline__ void pcr_tile(const PcrPassArgs& p, int64_t j, int64_
             }
         }
     } else {
+        // subsystem-major output: row t of subsystem r is row t >> K of
+        // subsystem r + (t mod 2^K) G at the next level's stride G 2^K
+        const int64_t G2 = p.G << p.K, q2 = nsys / G2, rem2 = nsys % G2;
+        const int64_t kmask = (int64_t(1) << p.K) - 1;
 #pragma unroll
         for (int q = 0; q < RPT; q++) {
             const int k = tid + q * bd;
             const int64_t t = t0 + k;
             if (k < TR && t >= wlo && t < whi) {
-                const int64_t gi = doff + t * dstep;
+                int64_t gi;
+                if (p.dst_sub) {
+                    const int64_t r2 = r + (t & kmask) * p.G;
+                    gi = dbase + r2 * q2 + min(r2, rem2) + (t >> p.K);
+                } else {
+                    gi = doff + t * dstep;
+                }
                 p.dst[A_][gi] = sa[k]; p.dst[B_][gi] = sb[k]; p.dst[C_][gi] = sc[k];
                 p.dst[D_][gi] = sd[k]; p.dst[E_][gi] = se[k]; p.dst[Y_][gi] = sy[k];
                 p.dst[AL1_][gi] = al1p[q]; p.dst[AL2_][gi] = al2p[q];

@@ -39,7 +39,12 @@ __host__ __device__ inline int ref_strides(int64_t n) {
 // One faithful global/shared pass over (sub)systems at decoupled level G.
 // Element (system j, subsystem r, local row t) of an array lives at
 //   (offsets ? offsets[j] : j*ss) + (r + t*G) * rs
-// with (ss, rs) = (n, 1) for the contiguous layout and (1, m) interleaved.
+// with (ss, rs) = (n, 1) for the contiguous layout and (1, m) interleaved;
+// or, in a subsystem-major array of a uniform batch (src_sub / dst_sub), at
+//   j*ss + r*(n/g) + min(r, n%g) + t
+// where g is the array's gather stride (G for src, G*2^K for dst): every
+// subsystem contiguous, so a pass reads its subsystem's rows in one run
+// instead of G*8 bytes apart.
 struct PcrPassArgs {
     const double* src[NSTATE];   // state in (A_/E_/AL1_/AL2_ may be null: zeros)
     double* dst[NSTATE];         // state out (non-final passes)
@@ -56,6 +61,8 @@ struct PcrPassArgs {
     int L;                       // rows written per window (local)
     int H;                       // halo rows on each side (local), 2*(2^K-1)
     int TRmax;                   // shared-memory rows per CTA (>= L + 2H, or whole subsystem)
+    int src_sub;                 // 1: src is subsystem-major at stride G (uniform batches)
+    int dst_sub;                 // 1: dst is subsystem-major at stride G*2^K (uniform batches)
 };
 
 // Host-side launchers (pcr_f64.cu).  `tridiagonal`: the batch entered with

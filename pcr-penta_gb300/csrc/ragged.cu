@@ -192,6 +192,7 @@ rg_persistent_kernel(RgArgs a)
             p.K = K[lvl]; p.final_step = fin ? 1 : 0; p.L = Lw[lvl]; p.H = H[lvl];
             p.nwin = nwin[lvl];
             p.TRmax = a.cap;
+            p.src_sub = 0; p.dst_sub = 0;             // ragged arrays keep the natural row order
             const int64_t r = fin ? i : i / nwin[lvl];
             const int64_t w = fin ? 0 : i - r * nwin[lvl];
             pcr_tile<kRgRPT, true>(p, k, r, w, smem);
