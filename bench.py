@@ -44,7 +44,7 @@ BYTES_PER_UNKNOWN = 56          # 5 FP64 bands + FP64 rhs read once, FP64 x writ
 # config's own layout and the autotuned plan.  The capture commands are in the
 # profiles named here.
 MEASURED_TRAFFIC = {
-    ("c1", "f64"): (517.0, "ncu capture m=48 n=65536, the 5 pcr_pass_kernel launches of one solve "
+    ("c1", "f64"): (495.4, "ncu capture m=48 n=65536, the 5 pcr_pass_kernel launches of one solve "
                            "(profiles/pcr_pass_kernel_f64_m256_n65536.md)"),
     ("c1", "mixed"): (133.2, "ncu capture m=48 n=65536, mp_first_kernel + mp_try_kernel of one solve "
                              "(profiles/mixed_kernels_m256_n65536.md)"),
