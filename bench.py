@@ -1,9 +1,10 @@
 """Benchmark of the batched pentadiagonal PCR-Penta solve on GB300.
 
-Default workload: plain FP64 PCR-Penta through pcrp_solve_f64 on m=256
-systems of n=65536 rows (the reference's large-n global path), seeded
-strictly diagonally dominant bands, contiguous (reference) layout, inputs
-resident in HBM.  Prints ONE JSON line (rank 0).
+Default workload: plain FP64 PCR-Penta through pcrp_solve_f64 on m=64
+systems of n=2^20 rows (the HBM-filling weakly dominant stress batch, the
+largest single-GPU workload), contiguous (reference) layout, inputs resident
+in HBM; the FP32+FP64-refinement solver is timed on the same inputs beside
+it.  Prints ONE JSON line (rank 0).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--config c0|c1|c2|c3|c4] [--solver f64|mixed]
@@ -11,12 +12,16 @@ resident in HBM.  Prints ONE JSON line (rank 0).
 Metric: Gunknowns/s = (systems x rows, all ranks) / device time per step.
 A step solves the whole batch once; it first restores the right-hand side
 with one device copy (16 B/unknown, named in `roofline.traffic_note`) because the
-solve overwrites y.  The inputs (0.8 GB at m=256, n=65536) exceed the 129 MB
+solve overwrites y.  The inputs (3.2 GB at m=64, n=2^20) exceed the 129 MB
 L2, so no L2 flush is needed between steps.
 
 --impl reference times the CPU restatement of the reference's PCR-Penta
 algorithm (oracle/, the reference has no CPU path of its own) on every host
-core, on a bounded sample of the same workload.
+core, on a bounded sample of the same workload; its inputs come from the
+oracle's own generator, so that arm never loads the product library.
+
+--gpus N without torchrun re-launches this script under
+torch.distributed.run with N ranks (one per GPU, 127.0.0.1 rendezvous).
 """
 from __future__ import annotations
 
@@ -41,15 +46,12 @@ BYTES_PER_UNKNOWN = 56          # 5 FP64 bands + FP64 rhs read once, FP64 x writ
 # smaller batch of the same systems (inputs still larger than L2), scaled to
 # the bench's batch by unknowns: systems are independent, so the traffic per
 # unknown does not depend on m.  Keyed by (config, solver); used only for the
-# config's own layout and the autotuned plan.  The capture commands are in the
-# profiles named here.
+# config's own layout and the autotuned plan.  The capture commands and the
+# raw figures are kept with the ncu summaries in the repository's profiles.
 MEASURED_TRAFFIC = {
-    ("c1", "f64"): (495.4, "ncu capture m=48 n=65536, the 5 pcr_pass_kernel launches of one solve "
-                           "(profiles/pcr_pass_kernel_f64_m256_n65536.md)"),
-    ("c1", "mixed"): (133.2, "ncu capture m=48 n=65536, mp_first_kernel + mp_try_kernel of one solve "
-                             "(profiles/mixed_kernels_m256_n65536.md)"),
-    ("c2", "mixed"): (123.0, "ncu capture m=1024 n=4096, the mp_small_kernel launch of one solve "
-                             "(profiles/mixed_small_kernel_c2_m4096_n4096.md)"),
+    ("c1", "f64"): (495.4, "ncu capture m=48 n=65536, the 5 pcr_pass_kernel launches of one solve"),
+    ("c1", "mixed"): (133.2, "ncu capture m=48 n=65536, mp_first_kernel + mp_try_kernel of one solve"),
+    ("c2", "mixed"): (123.0, "ncu capture m=1024 n=4096, the mp_small_kernel launch of one solve"),
 }
 
 
@@ -93,6 +95,12 @@ def fp64_ops(n: int):
         divs += 2 * pairs + max(min(df, n) - pairs, 0)
     return ops / n, divs / n
 
+
+GENERATORS = {0: "dominant: a,b,d,e ~ U[-1,1], c = sum|off| + U[1,2], y ~ U[-1,1]",
+              1: "ADI convection-diffusion (I - theta dt L), theta=0.5, dt=1e-3, r=0.03, payoff rhs",
+              2: "weakly dominant: a,b,d,e ~ U[-1,1], c = +-1.05 sum|off|, y ~ U[-1,1]"}
+SEED = 7
+L2_BYTES = 129 * 1000 * 1000     # GB300 L2 (inputs below twice this are flushed between steps)
 
 CONFIGS = {
     "c0": dict(m=1024, n=512, kind=0, layout="interleaved",
@@ -164,6 +172,31 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def config_dict(cfg, world):
+    """The workload description; both arms (ours, --impl reference) print the
+    same dict for the same --config and --gpus."""
+    m, n = cfg["m"], cfg["n"]
+    small = 48 * m * n < 2 * L2_BYTES
+    return {"workload": cfg["name"], "m": m, "n": n, "layout": cfg.get("layout", "contiguous"),
+            "generator": GENERATORS[cfg["kind"]], "seed": SEED,
+            "l2": (f"inputs ({48 * m * n / 1e6:.0f} MB) smaller than twice L2: a {2 * L2_BYTES / 1e6:.0f} MB "
+                   "write between timed steps, each step timed alone") if small else
+                  f"inputs larger than L2 ({48 * m * n / 1e9:.2f} GB vs {L2_BYTES / 1e6:.0f} MB), no flush",
+            "parallelism": f"replicas x{world} (independent systems per GPU)"}
+
+
+def relaunch_distributed(args):
+    """--gpus N > 1 outside torchrun: run this script again under
+    torch.distributed.run with N ranks on this node; returns its exit code."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
 def dist_setup(args):
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -179,9 +212,12 @@ def dist_setup(args):
 
 
 def cfg_layout(cfg):
-    """The workload's batch layout: interleaved (row-major over systems) or contiguous."""
-    import pcrp
-    return pcrp.INTERLEAVED if cfg.get("layout") == "interleaved" else pcrp.CONTIGUOUS
+    """The workload's batch layout: 1 interleaved (row-major over systems) or 0
+    contiguous (the library's and the oracle's layout codes)."""
+    return 1 if cfg.get("layout") == "interleaved" else 0
+
+
+_CPU_INPUTS = {}
 
 
 def cpu_sample_gunk(cfg, systems: int, min_s: float = 2.0, solver: str = "pcr"):
@@ -191,11 +227,13 @@ def cpu_sample_gunk(cfg, systems: int, min_s: float = 2.0, solver: str = "pcr"):
     accumulated.  Returns (Gunknowns/s, cores, seconds, repetitions)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    import pcrp
     m, n = systems, cfg["n"]
     lay = cfg_layout(cfg)
-    arrs = pcrp.generate(cfg["kind"], 7, m, n, lay)
-    O.lib()
+    key = (cfg["kind"], m, n, lay)
+    if key not in _CPU_INPUTS:          # generated once per sample, outside the timing
+        _CPU_INPUTS.clear()
+        _CPU_INPUTS[key] = O.generate(cfg["kind"], SEED, m, n, lay)
+    arrs = _CPU_INPUTS[key]
     cores = os.cpu_count() or 1
     total, reps = 0.0, 0
     while total < min_s or reps == 0:
@@ -226,12 +264,12 @@ def run_reference(args, world, rank):
     sample = (f"{systems} of {cfg['m']} systems (n={cfg['n']}) solved {reps}x (>= 2 s) per step, "
               f"{cores} host threads")
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": cfg["m"] * cfg["n"] / value / 1e6,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded counter-based generator)", "impl": "reference",
-        "config": {"workload": cfg["name"], "m": cfg["m"], "n": cfg["n"], "layout": cfg.get("layout", "contiguous"),
-                   "solver": "CPU restatement of the reference PCR-Penta (oracle/pcrp_oracle.c)"},
+        "config": config_dict(cfg, world),
+        "solver": "CPU restatement of the reference PCR-Penta algorithm (oracle/pcrp_oracle.c), all host threads",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -251,7 +289,7 @@ def run_ours(args, world, rank, local, pg):
     hbm, peak_kind = peaks()
 
     # inputs: this rank's shard of systems (weak scaling: m systems per GPU)
-    seed = 7 + rank
+    seed = SEED + rank
     lay = cfg_layout(cfg)
     arrs = [torch.empty(m * n, dtype=torch.float64, device=dev) for _ in range(6)]
     with torch.cuda.stream(stream):
@@ -285,8 +323,8 @@ def run_ours(args, world, rank, local, pg):
     ev1 = torch.cuda.Event(enable_timing=True)
     # inputs that fit in L2 are flushed between timed steps (a write larger
     # than L2), each step then timed alone
-    l2 = torch.cuda.get_device_properties(dev).L2_cache_size
-    small = 48 * m * n < 2 * l2
+    l2 = max(torch.cuda.get_device_properties(dev).L2_cache_size, L2_BYTES)
+    small = 48 * m * n < 2 * L2_BYTES
     flush = torch.empty(2 * l2 // 4 + 1024, dtype=torch.float32, device=dev) if small else None
     step_ms = []
     with ClockSampler(local) as clk:
@@ -521,13 +559,9 @@ def run_ours(args, world, rank, local, pg):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.solver == "f64" else "f32+f64",
         "data": "synthetic (seeded counter-based generator, generated on device)",
-        "config": {"workload": cfg["name"], "m": m, "n": n, "layout": cfg.get("layout", "contiguous"),
-                   "solver": "pcrp_solve_f64 (bit-faithful PCR-Penta)" if args.solver == "f64"
-                   else "pcrp_solve_mixed (FP32 block PCR + FP64 refinement)",
-                   "l2": (f"inputs ({48 * m * n / 1e6:.0f} MB) smaller than twice L2: a {2 * l2 / 1e6:.0f} MB "
-                          "write between timed steps, each step timed alone") if small else
-                         f"inputs larger than L2 ({48 * m * n / 1e9:.2f} GB vs {l2 / 1e6:.0f} MB), no flush",
-                   "parallelism": f"replicas x{world} (independent systems per GPU)"},
+        "config": config_dict(cfg, world),
+        "solver": "pcrp_solve_f64 (bit-faithful PCR-Penta)" if args.solver == "f64"
+                  else "pcrp_solve_mixed (FP32 block PCR + FP64 refinement)",
         "gpu_launches": launches,
         "opts": json.loads(args.opts) if args.opts else "autotuned defaults",
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 6 * 8 * m * n,
@@ -596,7 +630,7 @@ def run_ragged_bench(args, world, rank, local, pg):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     cfg = CONFIGS[args.config]
-    seed = 7 + rank
+    seed = SEED + rank
     sizes = pcrp.ragged_sizes(seed, cfg["m"], 32, 65536)
     offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
     total = int(offs[-1])
@@ -660,7 +694,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=sorted(CONFIGS), default="c1")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="c4")
     ap.add_argument("--solver", choices=["f64", "mixed"], default="f64")
     ap.add_argument("--ref-systems", type=int, default=64)
     ap.add_argument("--m", type=int, default=0, help="override the number of systems (profiling runs)")
@@ -678,6 +712,8 @@ def main():
     if args.m > 0:
         CONFIGS[args.config] = dict(CONFIGS[args.config], m=args.m)
         CONFIGS[args.config]["name"] += f" (m overridden to {args.m})"
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_distributed(args))
     world, rank, local, pg = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)

@@ -130,9 +130,11 @@ pcrp_status pcrp_solve_f64_split(const double* a, const double* b, const double*
  * (host callbacks and plugin hooks that may not enter the CUDA allocator,
  * hosts whose GPU memory is fixed at start-up).  Its scratch is a 64 MiB
  * array compiled into the library, which every GPU that loads the library
- * keeps until the process exits; a call therefore accepts at most
- * m*n <= 524288 unknowns and returns PCRP_EINVAL, with the limit in the error
- * text, for more.  It calls no allocator.  The first call on a device looks up
+ * keeps until the process exits.  Systems that fit the shared-memory tile
+ * (n <= 960 with the tuned plan) need no scratch and any batch of them is
+ * accepted; longer systems need 128 bytes of scratch per unknown, so a call
+ * of those accepts at most m*n <= 524288 unknowns and returns PCRP_EINVAL,
+ * with the limit in the error text, for more.  It calls no allocator.  The first call on a device looks up
  * the array's device address, so make one call per device before any stream
  * capture.  Calls share the array: calls whose GPU work overlaps in time race
  * on it, so order them on one stream.  Results are bit-identical to

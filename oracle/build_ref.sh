@@ -5,9 +5,10 @@
 # the GPU to produce golden outputs of the reference itself.
 #   kernel_nofma.ptx  built with -fmad=false (every product and sum rounded)
 #   kernel_fma.ptx    built with nvcc's default FMA contraction
-# Usage: oracle/build_ref.sh [reference_dir]   (default /root/reference)
+# Usage: oracle/build_ref.sh [reference_dir]
+#   (default: $PCRP_REFERENCE_DIR, else the read-only checkout at /root/reference)
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${PCRP_REFERENCE_DIR:-/root/reference}}
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
 mkdir -p "$OUT"

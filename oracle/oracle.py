@@ -8,6 +8,8 @@ and the CPU-baseline / reference leg of ``bench.py``; never by the product.
 * :func:`ge`  -- FP64 pentadiagonal Gaussian elimination (ground truth for
   diagonally dominant systems; no counterpart in the reference).
 * :func:`residual` -- r = y - A x with long-double accumulation.
+* :func:`generate` -- the seeded benchmark inputs (same values as the
+  library's generator, checked bit for bit in tests/test_oracle.py).
 """
 from __future__ import annotations
 
@@ -52,6 +54,9 @@ def lib() -> ctypes.CDLL:
         L.oracle_ragged_batch.restype = ctypes.c_int
         L.oracle_residual_batch.argtypes = six + [_dp, _dp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int]
         L.oracle_residual_batch.restype = ctypes.c_int
+        L.oracle_generate.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
+                                      ctypes.c_int] + six + [ctypes.c_int]
+        L.oracle_generate.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -111,6 +116,17 @@ def residual(a, b, c, d, e, y, x, m: int, n: int, layout: int = CONTIGUOUS) -> n
     r = np.zeros(m * n, dtype=np.float64)
     lib().oracle_residual_batch(*[_ptr(v) for v in arrs], _ptr(xx), _ptr(r), m, n, layout)
     return r
+
+
+def generate(kind: int, seed: int, m: int, n: int, layout: int = CONTIGUOUS, threads: int = 0):
+    """The seeded benchmark inputs (a, b, c, d, e, y), restated in C beside the
+    solvers so that CPU-only runs need not load the product library."""
+    arrs = [np.zeros(m * n, dtype=np.float64) for _ in range(6)]
+    rc = lib().oracle_generate(kind, seed & 0xFFFFFFFFFFFFFFFF, m, n, layout, *[_ptr(v) for v in arrs],
+                                threads)
+    if rc:
+        raise ValueError(f"oracle_generate: bad arguments (kind={kind}, m={m}, n={n})")
+    return arrs
 
 
 def fwd_err(x, xref, m: int, n: int, layout: int = CONTIGUOUS) -> float:

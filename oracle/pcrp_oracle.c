@@ -333,3 +333,127 @@ int oracle_residual_batch(const double* a, const double* b, const double* c, con
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* seeded inputs                                                       */
+/* ------------------------------------------------------------------ */
+
+/* The benchmark inputs, restated here so that the CPU leg of the benchmark
+ * (and the reference arm, which times this file's PCR restatement) never
+ * loads the product library.  Same definition as the library's generator:
+ * every value is a pure function of (seed, kind, system j, row i, n), drawn
+ * from SplitMix64 (Steele, Lea, Flood, "Fast splittable pseudorandom number
+ * generators", OOPSLA 2014) of a counter packing (stream, system, row).
+ * tests/test_oracle.py checks the two bit for bit.  kind: 0 dominant
+ * (a,b,d,e ~ U[-1,1], c = sum|off| + U[1,2]), 1 ADI convection-diffusion
+ * (M = I - theta dt L, theta = 0.5, dt = 1e-3, r = 0.03 on S in [0, 800]),
+ * 2 weakly dominant (c = +-1.05 sum|off|), 3 the reference's Toeplitz
+ * fixture (kernel.cu:19-24).  y ~ U[-1,1], or the payoff max(S-K, 0). */
+static uint64_t sm64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+static double g_unit(uint64_t seed, int stream, uint64_t j, uint64_t i)
+{
+    const uint64_t ctr = ((uint64_t)stream << 56) | ((j & 0xFFFFFFULL) << 32) | (i & 0xFFFFFFFFULL);
+    const uint64_t z = sm64(sm64(seed) + ctr * 0xD1B54A32D192ED03ULL);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+static double g_uniform(uint64_t seed, int stream, uint64_t j, uint64_t i, double lo, double hi)
+{
+    return lo + (hi - lo) * g_unit(seed, stream, j, i);
+}
+
+static void g_row(int kind, uint64_t seed, uint64_t j, int64_t i, int64_t n, double* v)
+{
+    const int hasA = i >= 2, hasB = i >= 1, hasD = i + 1 < n, hasE = i + 2 < n;
+    double a, b, c, d, e, y;
+    if (kind == 0 || kind == 2) {
+        a = hasA ? g_uniform(seed, 0, j, (uint64_t)i, -1.0, 1.0) : 0.0;
+        b = hasB ? g_uniform(seed, 1, j, (uint64_t)i, -1.0, 1.0) : 0.0;
+        d = hasD ? g_uniform(seed, 3, j, (uint64_t)i, -1.0, 1.0) : 0.0;
+        e = hasE ? g_uniform(seed, 4, j, (uint64_t)i, -1.0, 1.0) : 0.0;
+        const double off = ((fabs(a) + fabs(b)) + fabs(d)) + fabs(e);
+        if (kind == 0) {
+            c = off + g_uniform(seed, 2, j, (uint64_t)i, 1.0, 2.0);
+        } else {
+            const double sgn = (sm64(seed ^ 0x5EED5EED5EEDULL ^ (j << 32) ^ (uint64_t)i) >> 63) ? -1.0 : 1.0;
+            c = off != 0.0 ? sgn * (1.05 * off) : sgn;
+        }
+        y = g_uniform(seed, 5, j, (uint64_t)i, -1.0, 1.0);
+    } else if (kind == 1) {
+        const double vv = g_uniform(seed, 6, j, 0, 0.01, 1.0);
+        const double K = g_uniform(seed, 7, j, 0, 50.0, 150.0);
+        const double rr = 0.03, tdt = 0.5 * 1e-3;
+        const double h = n > 1 ? 800.0 / (double)(n - 1) : 800.0;
+        const double S = (double)i * h;
+        const double diff = ((0.5 * vv) * (S * S)) / (h * h);
+        const double conv = (rr * S) / (2.0 * h);
+        a = 0.0;
+        b = hasB ? -(tdt * diff) : 0.0;
+        c = 1.0 + tdt * (((2.0 * diff) + (3.0 * conv)) + rr);
+        d = hasD ? -(tdt * (diff + 4.0 * conv)) : 0.0;
+        e = hasE ? tdt * conv : 0.0;
+        const double pay = S - K;
+        y = pay > 0.0 ? pay : 0.0;
+    } else {
+        a = 1.0; b = -4.0; c = 6.0; d = -4.0; e = 1.0; y = 1.0;
+        if (i == 0) { a = 0.0; b = 1.0; c = 5.0; }
+        if (i == 1) a = 0.0;
+        if (i == n - 2) e = 0.0;
+        if (i == n - 1) { c = 5.0; d = 1.0; e = 0.0; }
+    }
+    v[0] = a; v[1] = b; v[2] = c; v[3] = d; v[4] = e; v[5] = y;
+}
+
+typedef struct {
+    int kind, layout;
+    uint64_t seed;
+    int64_t m, n, j0, j1;
+    double *a, *b, *c, *d, *e, *y;
+} gen_job_t;
+
+static void* gen_run(void* arg)
+{
+    const gen_job_t* g = (const gen_job_t*)arg;
+    for (int64_t j = g->j0; j < g->j1; j++)
+        for (int64_t i = 0; i < g->n; i++) {
+            double v[6];
+            const int64_t k = g->layout ? i * g->m + j : j * g->n + i;
+            g_row(g->kind, g->seed, (uint64_t)j, i, g->n, v);
+            g->a[k] = v[0]; g->b[k] = v[1]; g->c[k] = v[2]; g->d[k] = v[3]; g->e[k] = v[4]; g->y[k] = v[5];
+        }
+    return NULL;
+}
+
+/* Fills the six arrays of a batch (layout 0 contiguous, 1 interleaved),
+ * systems split over nthreads threads (<= 0: all cores). */
+int oracle_generate(int kind, uint64_t seed, int64_t m, int64_t n, int layout,
+                    double* a, double* b, double* c, double* d, double* e, double* y, int nthreads)
+{
+    if (kind < 0 || kind > 3 || m < 0 || n < 0) return -1;
+    if (nthreads <= 0) {
+        long cpus = sysconf(_SC_NPROCESSORS_ONLN);
+        nthreads = cpus > 0 ? (int)cpus : 1;
+    }
+    if (nthreads > m) nthreads = m > 0 ? (int)m : 1;
+    gen_job_t jobs[256];
+    pthread_t th[256];
+    if (nthreads > 256) nthreads = 256;
+    for (int t = 0; t < nthreads; t++) {
+        gen_job_t g = {kind, layout, seed, m, n, m * t / nthreads, m * (t + 1) / nthreads, a, b, c, d, e, y};
+        jobs[t] = g;
+        if (nthreads == 1 || pthread_create(&th[t], NULL, gen_run, &jobs[t]) != 0) {
+            gen_run(&jobs[t]);
+            th[t] = 0;
+        }
+    }
+    for (int t = 0; t < nthreads; t++)
+        if (nthreads > 1 && th[t]) pthread_join(th[t], NULL);
+    return 0;
+}

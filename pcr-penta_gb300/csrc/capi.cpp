@@ -71,6 +71,14 @@ pcrp_status get_workspace(const pcrp_opts* o, size_t bytes, cudaStream_t s, void
     std::lock_guard<std::mutex> lk(g_ws_mu);
     auto& slot = g_ws[{dev, s}];
     if (slot.second < bytes) {
+        // growing means a stream synchronisation and a cudaMalloc, neither of
+        // which a stream under capture allows
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+            return set_error(PCRP_ENOTSUP,
+                             "the library workspace of this stream must grow to %zu bytes, which cannot happen "
+                             "during stream capture: make one call of this size before capturing, or pass "
+                             "opts->workspace", bytes);
         if (slot.first) {
             e = cudaStreamSynchronize(s);
             if (e != cudaSuccess) return cuda_error(e, "cudaStreamSynchronize (workspace growth)");
@@ -126,6 +134,13 @@ static int split_strides(int64_t n, int smem_rows)
 
 size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_sweeps, bool info, int32_t layout);
 
+// Whether a solve of n-row systems with these options runs global passes
+// (and so needs split-path scratch); n <= the shared-memory tile needs none.
+bool f64_needs_scratch(int64_t n, const pcrp_opts* o)
+{
+    return split_strides(n, f64_plan(o, n).smem_rows) > 0;
+}
+
 size_t f64_workspace_bytes(int64_t m, int64_t n, int32_t layout, const F64Plan& pl, bool split)
 {
     (void)layout;
@@ -151,6 +166,9 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
     if (!b || !c || !d || !y) return set_error(PCRP_EINVAL, "%s: null array (only a and e may be null)", who);
     if (n > (int64_t(1) << 31) || m > (int64_t(1) << 40))
         return set_error(PCRP_EINVAL, "%s: size out of range", who);
+    if (m > (int64_t(1) << 52) / (2 * NSTATE * (int64_t)sizeof(double)) / n)
+        return set_error(PCRP_EINVAL, "%s: m*n = %lld * %lld is too large for the split-path scratch", who,
+                         (long long)m, (long long)n);
 
     // null a and e: a tridiagonal batch, both bands +0.0; the first pass
     // reads neither, and every pass runs the zero-state strides
@@ -176,6 +194,7 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
         const size_t need = 2 * (size_t)NSTATE * (size_t)m * (size_t)n * sizeof(double);
         pcrp_status rc = get_workspace(o, need, st, &ws);
         if (rc != PCRP_OK) return rc;
+        if (!ws) return set_error(PCRP_ENOMEM, "%s: no scratch for the split path (%zu bytes)", who, need);
         double* base = static_cast<double*>(ws);
         for (int u = 0; u < 2; u++)
             for (int k = 0; k < NSTATE; k++) bufs[u][k] = base + ((size_t)u * NSTATE + k) * (size_t)(m * n);

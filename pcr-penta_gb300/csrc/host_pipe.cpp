@@ -29,9 +29,13 @@ namespace {
 constexpr int kMaxDev = 64;
 std::mutex g_mu;
 cudaStream_t g_streams[kMaxDev][2] = {};
-cudaEvent_t g_events[kMaxDev][3] = {};
+// One host thread at a time enqueues onto a device's internal streams: the
+// solver scratch of each internal stream is a growing library buffer, and a
+// growth started by one call between another call's lookup of that buffer
+// and its launches would free memory those launches still use.
+std::mutex g_enqueue_mu[kMaxDev];
 
-pcrp_status dev_streams(int dev, cudaStream_t* s, cudaEvent_t* ev)
+pcrp_status dev_streams(int dev, cudaStream_t* s)
 {
     if (dev < 0 || dev >= kMaxDev) return set_error(PCRP_ENOTSUP, "pcrp_solve_host: device %d", dev);
     std::lock_guard<std::mutex> lk(g_mu);
@@ -40,15 +44,28 @@ pcrp_status dev_streams(int dev, cudaStream_t* s, cudaEvent_t* ev)
             cudaError_t e = cudaStreamCreateWithFlags(&g_streams[dev][k], cudaStreamNonBlocking);
             if (e != cudaSuccess) return cuda_error(e, "cudaStreamCreate");
         }
-        for (int k = 0; k < 3; k++) {
-            cudaError_t e = cudaEventCreateWithFlags(&g_events[dev][k], cudaEventDisableTiming);
-            if (e != cudaSuccess) return cuda_error(e, "cudaEventCreate");
-        }
     }
     s[0] = g_streams[dev][0]; s[1] = g_streams[dev][1];
-    for (int k = 0; k < 3; k++) ev[k] = g_events[dev][k];
     return PCRP_OK;
 }
+
+// The three join events of one call (caller -> internal streams, internal
+// streams -> caller).  Each call owns its events: shared ones would let a
+// concurrent call on another caller stream re-record the fork event between
+// this call's record and its waits, so the internal streams would skip work
+// the caller queued before the call.  An event may be destroyed as soon as
+// its waits are enqueued (the runtime releases it once it completes).
+struct CallEvents {
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    cudaError_t create() {
+        for (auto& e : ev) {
+            const cudaError_t rc = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+            if (rc != cudaSuccess) return rc;
+        }
+        return cudaSuccess;
+    }
+    ~CallEvents() { for (auto e : ev) if (e) cudaEventDestroy(e); }
+};
 
 // copy systems [j0, j0+mc) of a host batch (layout) into / out of a device chunk
 cudaError_t copy_chunk(double* dst, const double* src, int64_t j0, int64_t mc, int64_t m, int64_t n,
@@ -89,9 +106,13 @@ extern "C" pcrp_status pcrp_solve_host(const double* a, const double* b, const d
     cudaError_t ce = cudaGetDevice(&dev);
     if (ce != cudaSuccess) return cuda_error(ce, "cudaGetDevice");
     cudaStream_t S[2];
-    cudaEvent_t E[3];
-    pcrp_status rc = dev_streams(dev, S, E);
+    pcrp_status rc = dev_streams(dev, S);
     if (rc != PCRP_OK) return rc;
+    std::lock_guard<std::mutex> enqueue_lock(g_enqueue_mu[dev]);
+    CallEvents CE;
+    ce = CE.create();
+    if (ce != cudaSuccess) return cuda_error(ce, "pcrp_solve_host: cudaEventCreate");
+    cudaEvent_t* E = CE.ev;
 
     // chunk sizes: ceil(m/32) systems, then x3 per chunk up to ceil(m/4);
     // at most 2^26 unknowns each

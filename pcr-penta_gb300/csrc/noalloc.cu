@@ -28,8 +28,12 @@
 namespace pcrp {
 
 // Scratch of the split path: two ping-pong copies of the 8-array pass state
-// (128 bytes per unknown), so this size limits one call to m*n <= 524288.
+// (128 bytes per unknown), so this size limits one call of systems longer
+// than the shared-memory tile (n > 960 with the tuned plan) to
+// m*n <= 524288.  Shorter systems are solved whole in shared memory, need
+// no scratch, and have no limit.
 constexpr size_t kPcrpNoallocScratchBytes = size_t(64) << 20;   // 64 MiB
+constexpr int64_t kPcrpNoallocMaxUnknowns = (int64_t)(kPcrpNoallocScratchBytes / (2 * NSTATE * sizeof(double)));
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kPcrpNoallocScratchBytes];
 
@@ -37,6 +41,7 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
                       const double* e, double* y, int64_t m, int64_t n, int32_t layout,
                       const pcrp_opts* o, cudaStream_t st, bool force_small, bool force_split,
                       const char* who);
+bool f64_needs_scratch(int64_t n, const pcrp_opts* o);
 
 namespace {
 constexpr int kMaxDevices = 64;
@@ -71,21 +76,25 @@ extern "C" pcrp_status pcrp_solve_f64_noalloc(const double* a, const double* b, 
                                               int64_t m, int64_t n, int32_t layout, pcrp_stream stream)
 {
     if (m < 0 || n < 0) return set_error(PCRP_EINVAL, "pcrp_solve_f64_noalloc: negative size");
-    const size_t need = 2 * (size_t)NSTATE * (size_t)m * (size_t)n * sizeof(double);
-    if (need > kPcrpNoallocScratchBytes)
-        return set_error(PCRP_EINVAL,
-                         "pcrp_solve_f64_noalloc: m*n = %lld needs %zu bytes of scratch, more than the "
-                         "library's fixed %zu bytes (m*n <= %zu); use pcrp_solve_f64 with a workspace",
-                         (long long)(m * n), need, kPcrpNoallocScratchBytes,
-                         kPcrpNoallocScratchBytes / (2 * NSTATE * sizeof(double)));
     if (m == 0 || n == 0) return PCRP_OK;
+    pcrp_opts o{};
+    o.size = sizeof(pcrp_opts);
+    // Systems that fit the shared-memory tile are solved whole and touch no
+    // scratch, so only the split path has a size limit.  (Compared without
+    // forming m*n, which could wrap for huge sizes.)
+    if (f64_needs_scratch(n, &o) && m > kPcrpNoallocMaxUnknowns / n)
+        return set_error(PCRP_EINVAL,
+                         "pcrp_solve_f64_noalloc: m=%lld systems of n=%lld rows need %.0f bytes of scratch, "
+                         "more than the library's fixed %zu bytes (m*n <= %lld for n above the "
+                         "shared-memory tile); use pcrp_solve_f64 with a workspace",
+                         (long long)m, (long long)n, 2.0 * NSTATE * sizeof(double) * (double)m * (double)n,
+                         kPcrpNoallocScratchBytes, (long long)kPcrpNoallocMaxUnknowns);
     void* scratch = nullptr;
     pcrp_status rc = noalloc_scratch(&scratch);
     if (rc != PCRP_OK) return rc;
-    // Every pass writes all the rows a later pass reads, so the scratch needs no
-    // clearing; it keeps the previous call's contents.
-    pcrp_opts o{};
-    o.size = sizeof(pcrp_opts);
+    // Every pass writes all the rows a later pass reads, so the scratch needs
+    // no clearing; it keeps the previous call's contents.  A caller-provided
+    // workspace is never grown, so nothing below can allocate.
     o.workspace = scratch;
     o.workspace_bytes = kPcrpNoallocScratchBytes;
     return f64_solve(a, b, c, d, e, y, m, n, layout, &o, (cudaStream_t)stream, false, false,

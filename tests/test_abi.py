@@ -122,3 +122,28 @@ def test_mixed_workspace_includes_layout_adapter(built_lib):
         ii = pcrp.workspace_size(m, n, pcrp.INTERLEAVED, which=1)
         assert ii - ci == 6 * arr
     assert pcrp.workspace_size(1, 5000, pcrp.INTERLEAVED, which=1) == pcrp.workspace_size(1, 5000, pcrp.CONTIGUOUS, which=1)
+
+
+def test_noalloc_size_checks_do_not_wrap(built_lib):
+    """The allocation-free entry point checks its fixed scratch without
+    forming m*n (which could wrap around) and refuses before any CUDA call."""
+    L = pcrp.lib()
+    for m, n in ((1 << 33, 1 << 27), (1 << 40, 1 << 31), (3, 1 << 20), (9, 65536)):
+        assert L.pcrp_solve_f64_noalloc(1, 1, 1, 1, 1, 1, m, n, 0, None) == 1, (m, n)
+        assert "524288" in pcrp.last_error()
+    for fn in ("pcrp_solve_f64", "pcrp_solve_f64_split"):
+        # the split path's own scratch size is checked the same way
+        assert getattr(L, fn)(1, 1, 1, 1, 1, 1, 1 << 40, 1 << 31, 0, None, None) == 1
+        assert "too large" in pcrp.last_error() or "out of range" in pcrp.last_error()
+
+
+def test_noalloc_accepts_any_batch_of_short_systems_on_cpu(built_lib):
+    """Systems that fit the shared-memory tile need no scratch, so no size
+    limit applies to them: without a GPU the call gets past the size check
+    and fails only at the first CUDA call (PCRP_ECUDA, not PCRP_EINVAL)."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("CPU-only check (fake pointers); the GPU test solves such a batch for real")
+    L = pcrp.lib()
+    rc = L.pcrp_solve_f64_noalloc(8, 8, 8, 8, 8, 8, 1 << 20, 512, 0, None)
+    assert rc == 2, pcrp.last_error()

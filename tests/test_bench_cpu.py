@@ -76,22 +76,79 @@ def dram_mb(path, names):
     return tot
 
 
+# the ncu summaries the bench's traffic table was read from
+PROFILES = {("c1", "f64"): "profiles/pcr_pass_kernel_f64_m256_n65536.md",
+            ("c1", "mixed"): "profiles/mixed_kernels_m256_n65536.md",
+            ("c2", "mixed"): "profiles/mixed_small_kernel_c2_m4096_n4096.md"}
+
+
 @pytest.mark.parametrize("key,col_names,units", [
     (("c1", "f64"), ["dram__bytes_read.sum (MB)", "dram__bytes_write.sum (MB)"], 48 * 65536),
     (("c1", "mixed"), ["dram__bytes_read.sum (MB)", "dram__bytes_write.sum (MB)"], 48 * 65536),
 ])
 def test_measured_traffic_matches_profiles(key, col_names, units):
     """The bench's DRAM bytes per unknown equal the committed captures' sums."""
-    per, note = bench.MEASURED_TRAFFIC[key]
-    prof = os.path.join(bench.ROOT, note.split("(")[-1].rstrip(")"))
-    got = dram_mb(prof, col_names) * 1e6 / units
+    per, _ = bench.MEASURED_TRAFFIC[key]
+    got = dram_mb(os.path.join(bench.ROOT, PROFILES[key]), col_names) * 1e6 / units
     assert abs(got - per) < 0.5, (got, per)
 
 
 def test_measured_traffic_c2_matches_profile():
-    per, note = bench.MEASURED_TRAFFIC[("c2", "mixed")]
-    prof = os.path.join(bench.ROOT, note.split("(")[-1].rstrip(")"))
-    with open(prof) as f:
+    per, _ = bench.MEASURED_TRAFFIC[("c2", "mixed")]
+    with open(os.path.join(bench.ROOT, PROFILES[("c2", "mixed")])) as f:
         row = next(line for line in f if line.startswith("| dram__bytes_read / write (MB)"))
     rd, wr = [float(v) for v in row.split("|")[2].split("/")]   # the current kernel's column
     assert abs((rd + wr) * 1e6 / (1024 * 4096) - per) < 0.5
+
+
+def test_bench_messages_name_no_files():
+    """Printed notes describe captures in words, not by repository paths."""
+    for per, note in bench.MEASURED_TRAFFIC.values():
+        assert "profiles/" not in note and ".md" not in note
+
+
+def run_bench(*args, timeout=600):
+    import json
+    import subprocess
+    env = dict(os.environ)
+    env.pop("WORLD_SIZE", None)
+    out = subprocess.run([sys.executable, os.path.join(bench.ROOT, "bench.py"), *args], capture_output=True,
+                         text=True, timeout=timeout, env=env)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    return [json.loads(ln) for ln in lines]
+
+
+def test_reference_arm_config_matches_ours_and_default_is_c4():
+    """Both arms print the same config dict; the default workload is the
+    largest single-GPU configuration (m=64, n=2^20)."""
+    ref = bench.config_dict(bench.CONFIGS["c4"], 1)
+    assert ref["m"] == 64 and ref["n"] == 1 << 20 and "solver" not in ref
+    import argparse  # noqa: F401
+    src = open(os.path.join(bench.ROOT, "bench.py")).read()
+    assert 'choices=sorted(CONFIGS), default="c4"' in src
+    assert src.count('"config": config_dict(cfg, world)') == 2
+
+
+def test_reference_arm_two_ranks_one_line():
+    """--impl reference --gpus 2 outside torchrun launches two gloo ranks
+    itself; rank 0 alone prints one line with n_gpus 2 and never loads the
+    product library."""
+    lines = run_bench("--impl", "reference", "--config", "c0", "--gpus", "2", "--steps", "1", "--warmup", "3",
+                      "--ref-systems", "4")
+    assert len(lines) == 1
+    ln = lines[0]
+    assert ln["impl"] == "reference" and ln["n_gpus"] == 2
+    assert ln["config"] == bench.config_dict(bench.CONFIGS["c0"], 2)
+    assert ln["e2e"]["h2d_bytes_per_step"] == 0 and ln["cpu_baseline"]["kind"] == "port"
+
+
+def test_reference_arm_does_not_load_libpcrp():
+    """The CPU reference arm generates its inputs with the oracle."""
+    import subprocess
+    code = ("import sys, runpy; sys.argv=['bench.py','--impl','reference','--config','c0','--steps','1',"
+            "'--warmup','3','--ref-systems','2']; runpy.run_path('bench.py', run_name='__main__');"
+            "maps=open('/proc/self/maps').read(); print('LOADED' if 'libpcrp.so' in maps else 'CLEAN')")
+    out = subprocess.run([sys.executable, "-c", code], cwd=bench.ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.strip().splitlines()[-1] == "CLEAN"

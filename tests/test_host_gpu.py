@@ -54,3 +54,43 @@ def test_host_mixed_meets_tolerance_pageable(cuda):
     pcrp.solve_host(*h, m, n, precision=1)
     torch.cuda.synchronize()
     assert O.fwd_err(h[5], O.ge(*arrs, m, n), m, n) <= 1e-12
+
+
+def test_host_concurrent_calls_on_two_streams(cuda):
+    """Two host threads call pcrp_solve_host at once, each on its own caller
+    stream, each right after queueing a device->host copy that fills its host
+    right-hand side.  Each call must wait for its own stream's earlier work
+    (its join events belong to the call) and return the device solve's bits."""
+    import threading
+
+    import torch
+    m, n = 12, 3000
+    cases = []
+    for k in range(2):
+        arrs = dd_bands(np.random.default_rng(100 + k), m, n)
+        xd, _ = gpu_f64(arrs, m, n)
+        h = [torch.from_numpy(v.copy()).pin_memory() for v in arrs]
+        h[5].zero_()                                    # filled by the stream copy below
+        y_dev = torch.from_numpy(arrs[5]).to(cuda)
+        cases.append((h, y_dev, xd, torch.cuda.Stream()))
+    errors = []
+
+    def worker(k):
+        h, y_dev, xd, st = cases[k]
+        try:
+            for _ in range(4):
+                with torch.cuda.stream(st):
+                    torch.cuda._sleep(2000000)          # the copy below lands late
+                    h[5].copy_(y_dev, non_blocking=True)
+                    pcrp.solve_host(*h, m, n, precision=0, stream=st)
+                st.synchronize()
+                assert_bitexact(h[5].numpy(), xd, f"thread {k}")
+        except Exception as ex:                         # reported by the main thread
+            errors.append(ex)
+
+    th = [threading.Thread(target=worker, args=(k,)) for k in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors, errors[0]

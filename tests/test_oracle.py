@@ -185,3 +185,16 @@ def test_ragged_oracle_matches_uniform():
         for k, s in enumerate(sizes):
             sl_ = slice(offs[k], offs[k + 1])
             assert np.array_equal(xr[sl_], fn(*[v[sl_] for v in arrs], 1, int(s)))
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2, 3])
+@pytest.mark.parametrize("layout", [0, 1])
+def test_oracle_generator_equals_library_generator(kind, layout):
+    """The oracle's restated generator (used by the CPU legs of bench.py so
+    that they never load libpcrp.so) gives the library generator's bits."""
+    pcrp = pytest.importorskip("pcrp")
+    for m, n in [(3, 1), (4, 7), (5, 4096), (2, 65536)]:
+        ours = pcrp.generate(kind, 7, m, n, layout)
+        theirs = O.generate(kind, 7, m, n, layout)
+        for u, v in zip(ours, theirs):
+            assert np.array_equal(np.asarray(u).view(np.uint64), v.view(np.uint64))
