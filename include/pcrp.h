@@ -49,7 +49,8 @@ typedef enum pcrp_status {
     PCRP_EINVAL = 1,   /* bad argument (null pointer, negative size, n outside the path's range, bad layout) */
     PCRP_ECUDA = 2,    /* a CUDA runtime call or kernel launch failed                                    */
     PCRP_ENOMEM = 3,   /* scratch allocation failed, or opts->workspace is smaller than required          */
-    PCRP_ETIMEOUT = 4, /* a bounded device-side wait gave up (persistent ragged kernel)                   */
+    PCRP_ETIMEOUT = 4, /* a bounded device-side wait gave up (persistent ragged kernel, or a staging wait
+                          of the mixed solver's fused first sweeps; that solve still completes)           */
     PCRP_ENOCONV = 5,  /* iterative refinement did not reach tol within max_sweeps                        */
     PCRP_ENOTSUP = 6   /* unsupported combination of options                                              */
 } pcrp_status;
@@ -67,8 +68,10 @@ typedef struct pcrp_opts {
     int32_t  fuse_strides;     /* PCR strides fused per global-memory pass (n > smem_rows)   */
     int32_t  tile_rows;        /* rows written per CTA in a global pass                      */
     int32_t  threads;          /* threads per CTA                                            */
-    int32_t  reserved0;        /* 0; 0x7E57 makes pcrp_solve_ragged's first dependency wait
-                                  unsatisfiable (bounded, ~4 ms) to test PCRP_ETIMEOUT       */
+    int32_t  reserved0;        /* 0; 0x7E57 makes pcrp_solve_ragged's first dependency wait,
+                                  and the first staging wait of pcrp_solve_mixed's fused
+                                  first sweeps, unsatisfiable (bounded, ~4 ms) to test
+                                  PCRP_ETIMEOUT                                              */
     void*    workspace;        /* caller-provided device scratch, or NULL                    */
     size_t   workspace_bytes;
     int32_t  window_levels;    /* pcrp_solve_mixed, systems larger than one shared-memory
@@ -162,7 +165,13 @@ pcrp_status pcrp_solve_f64_noalloc(const double* a, const double* b, const doubl
  * PCRP_NO_GRAPH: always host-driven launches).  An interleaved batch of more
  * than one system is transposed into contiguous copies in the workspace,
  * solved there and transposed back (same result bits as the contiguous solve;
- * pcrp_workspace_size counts the copies).
+ * pcrp_workspace_size counts the copies).  Systems longer than one shared-
+ * memory tile (n > 4096), of even n with 16-byte aligned arrays, can run
+ * their first two sweeps in one fused pass over the inputs (windows with
+ * halos, inputs staged by bulk asynchronous copies, the tile's factorisation
+ * kept in tensor memory; environment variable PCRP_DUO=1, off by default);
+ * systems that pass need no other kernel, the rest are solved from the start
+ * by the general kernels.
  * No counterpart in the reference (new work named by the solver's design). */
 pcrp_status pcrp_solve_mixed(const double* a, const double* b, const double* c,
                              const double* d, const double* e, double* y,

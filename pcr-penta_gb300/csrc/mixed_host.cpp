@@ -50,8 +50,8 @@ MpPlan mp_plan(int64_t nb, const pcrp_opts* o)
 }
 
 struct MpLayout {
-    size_t S0, R, Mi, P0, P1, dx, X0, Yc, Xout, ctr, ndx, nx, fin, status, est, trunc, ndx_pre, live, fail, nfail, rbuf, rn,
-        total;
+    size_t S0, R, Mi, P0, P1, dx, X0, Yc, Xout, ctr, ndx, nx, fin, status, est, trunc, ndx_pre, live, fail, nfail, dnorm,
+        err, rbuf, rn, total;
 };
 
 MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool info)
@@ -80,6 +80,8 @@ MpLayout mp_layout(int64_t m, int64_t n, int max_sweeps, const MpPlan& pl, bool 
     L.live = take((size_t)(max_sweeps + 1) * sizeof(int));
     L.fail = take(m * sizeof(int));
     L.nfail = take(sizeof(int));
+    L.dnorm = take(2 * (size_t)m * sizeof(unsigned));
+    L.err = take(sizeof(int));
     L.rbuf = info ? take((size_t)m * n * sizeof(double)) : 0;
     L.rn = info ? take(3 * m * sizeof(unsigned)) : 0;
     L.total = off;
@@ -94,6 +96,8 @@ struct SweepPlan {
     MpWindows W;
     int64_t nb, T;
     bool windowed, cr_mode, fused;
+    bool duo;                   // sweeps 0 and 1 of every system run first in mp_duo_kernel (mixed_duo.cu);
+    DuoGeom D;                  // the general kernels then take only the systems it leaves
     float* P[2];                // ping-pong state of the block-PCR passes
 };
 
@@ -206,7 +210,7 @@ struct GraphKey {
     const void* ptr[8];
     int64_t m, n, ss, rs;
     double tol;
-    int max_sweeps, cap, fuse, win;
+    int max_sweeps, cap, fuse, win, duo;
     bool operator<(const GraphKey& o) const { return std::memcmp(this, &o, sizeof(GraphKey)) < 0; }
 };
 
@@ -239,16 +243,24 @@ int graph_mode(cudaStream_t st)
 // version or device refuses a step (the capture is then unusable).
 bool capture_sweep_loop(const MpArgs& A, const SweepPlan& S, cudaStream_t st)
 {
-    if (launch_mp_init(A, st) != cudaSuccess) return false;
-    if ((S.fused ? launch_mp_first(A, S.W, st) : launch_mp_prep(A, st)) != cudaSuccess) return false;
     cudaStreamCaptureStatus status;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t* deps = nullptr;
     size_t ndeps = 0;
     cudaGraphConditionalHandle h = 0;
-    if (cudaStreamGetCaptureInfo(st, &status, nullptr, &g, &deps, nullptr, &ndeps) != cudaSuccess ||
+    // with the fused first sweeps, the loop runs only if the gate kernel
+    // finds a system left; otherwise at least one sweep runs
+    if (cudaStreamGetCaptureInfo(st, &status, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess ||
         status != cudaStreamCaptureStatusActive ||
-        cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess)
+        cudaGraphConditionalHandleCreate(&h, g, S.duo ? 0 : 1, cudaGraphCondAssignDefault) != cudaSuccess)
+        return false;
+    if (launch_mp_init(A, st) != cudaSuccess) return false;
+    if (S.duo && (launch_mp_duo(A, S.D, st) != cudaSuccess || launch_mp_duo_finish(A, st) != cudaSuccess))
+        return false;
+    if ((S.fused ? launch_mp_first(A, S.W, st) : launch_mp_prep(A, st)) != cudaSuccess) return false;
+    if (S.duo && launch_mp_gate(A, h, st) != cudaSuccess) return false;
+    if (cudaStreamGetCaptureInfo(st, &status, nullptr, &g, &deps, nullptr, &ndeps) != cudaSuccess ||
+        status != cudaStreamCaptureStatusActive)
         return false;
     cudaGraphNodeParams cp{};
     cp.type = cudaGraphNodeTypeConditional;
@@ -310,7 +322,7 @@ pcrp_status launch_sweep_graph(const MpArgs& A, const SweepPlan& S, cudaStream_t
     const void* ptrs[8] = {A.a, A.b, A.c, A.d, A.e, A.y, A.S0, A.xout};
     for (int i = 0; i < 8; i++) k.ptr[i] = ptrs[i];
     k.m = A.m; k.n = A.n; k.ss = A.ss; k.rs = A.rs; k.tol = A.tol; k.max_sweeps = A.max_sweeps;
-    k.cap = S.pl.cap; k.fuse = S.pl.fuse; k.win = S.pl.win;
+    k.cap = S.pl.cap; k.fuse = S.pl.fuse; k.win = S.pl.win; k.duo = S.duo;
     std::lock_guard<std::mutex> lk(g_graph_mu);
     auto it = g_graphs.find(k);
     if (it == g_graphs.end()) {
@@ -389,6 +401,9 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     A.live = reinterpret_cast<int*>(base + WL.live);
     A.fail = reinterpret_cast<int*>(base + WL.fail);
     A.nfail = reinterpret_cast<int*>(base + WL.nfail);
+    A.dnorm = U(WL.dnorm);
+    A.err = reinterpret_cast<int*>(base + WL.err);
+    A.inject = (opts && opts->size >= sizeof(pcrp_opts) && opts->reserved0 == 0x7E57) ? 1 : 0;
     A.max_sweeps = max_sweeps; A.tol = (float)tol; A.keep_x = keep_x;
     {
         const void* ptrs[6] = {a, b, c, d, e, y};
@@ -405,6 +420,7 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     // Systems that fit one shared-memory tile: every sweep of a system in one
     // CTA, the whole solve one launch (no sweep loop to drive)
     if (pl.s1 == 0) {
+        A.err = nullptr;                          // (no fused pass, no status word)
         if (dest && !keep_x) {
             A.xout = dest->x; A.oss = dest->ss; A.ors = dest->rs;
             if (dest_written) *dest_written = true;
@@ -430,6 +446,11 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     S.fused = max_sweeps >= 2 && S.cr_mode;
     A.first_fused = S.fused;
     A.cr_mode = S.cr_mode;
+    // Sweeps 0 and 1 in one pass over the inputs for every system whose
+    // windows decouple (contiguous, even n, aligned arrays); mp_first and
+    // the sweep loop then see only the systems it leaves.
+    S.duo = S.fused && duo_plan(A, pl.win, &S.D);
+    if (!S.duo) A.err = nullptr;                 // (the status word belongs to the fused pass)
     S.P[0] = pl.s1 > 0 ? F(WL.P0) : nullptr;
     S.P[1] = pl.npass > 1 ? F(WL.P1) : nullptr;
     A.ctr = reinterpret_cast<int*>(base + WL.ctr);
@@ -452,6 +473,11 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
     A.ctr = nullptr;
     ce = launch_mp_init(A, st);
     if (ce != cudaSuccess) return cuda_error(ce, "mixed init launch");
+    if (S.duo) {
+        ce = launch_mp_duo(A, S.D, st);
+        if (ce == cudaSuccess) ce = launch_mp_duo_finish(A, st);
+        if (ce != cudaSuccess) return cuda_error(ce, "mixed fused-sweeps launch");
+    }
     ce = S.fused ? launch_mp_first(A, S.W, st) : launch_mp_prep(A, st);
     if (ce != cudaSuccess) return cuda_error(ce, S.fused ? "mixed first-sweep launch" : "mixed prep launch");
     for (int s = 0; s < max_sweeps; s++) {
@@ -550,8 +576,13 @@ extern "C" pcrp_status pcrp_solve_mixed(const double* a, const double* b, const 
     ce = cudaMemcpyAsync(conv.data(), A.status, m * sizeof(int), cudaMemcpyDeviceToHost, st);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(sw.data(), A.fin, m * sizeof(int), cudaMemcpyDeviceToHost, st);
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(est.data(), A.est, m * sizeof(float), cudaMemcpyDeviceToHost, st);
+    int waits_gave_up = 0;
+    if (ce == cudaSuccess && A.err)
+        ce = cudaMemcpyAsync(&waits_gave_up, A.err, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) return cuda_error(ce, "mixed report");
+    if (waits_gave_up)
+        return set_error(PCRP_ETIMEOUT, "%s: a staging wait of the fused first sweeps gave up (time limit)", who);
     int all = 1, maxsw = 0;
     float maxest = 0.0f;
     for (int64_t j = 0; j < m; j++) {

@@ -43,6 +43,9 @@ struct MpArgs {
     int* live;                          // [max_sweeps + 1] systems still running at the start of each sweep
     int* fail;                          // [m] 1: the windowed cyclic-reduction pass leaves the system coupled
     int* nfail;                         // systems with fail set
+    unsigned* dnorm;                    // [2 x m] fused first two sweeps: max |dx_0| (= max |x_0|), max |dx_1|
+    int* err;                           // nonzero: a bounded wait of the fused kernel gave up (null: no fused pass)
+    int inject;                         // test hook: the fused kernel never stages its first chunk
     int sweep, max_sweeps, keep_x;
     int vec;                            // 1: all six caller arrays are 16-byte aligned (paired loads allowed)
     int first_fused;                    // sweep 0 ran as mp_first_kernel (the refinement of sweep 0 only
@@ -118,6 +121,15 @@ struct MpWindows {
     int L, H, K, TRmax;                 // core rows, halo rows each side, levels (31: whole system), tile rows
 };
 
+// Window geometry of the fused first two sweeps (mixed_duo.cu), in block
+// rows: core windows of L rows; sweep 1 needs the level-0 rows within R of
+// the core (R = 2^(K+1) - 2 for K truncation levels), hence x_0 within R + 1
+// and so a tile halo of H >= 2R + 1 for sweep 0.
+struct DuoGeom {
+    int64_t nb, nwin;
+    int L, H, R, K;
+};
+
 // Where a solve that runs as one whole-system launch writes x when that is
 // not its y (the caller's interleaved y behind the layout adapter): the
 // kernel's final copy scatters x there, which takes the place of the
@@ -145,6 +157,14 @@ cudaError_t launch_mp_xupdate(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_decide(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_residual(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_advance(const MpArgs& p, cudaGraphConditionalHandle h, cudaStream_t s);
+// Fused sweeps 0 and 1 (mixed_duo.cu): whether a batch qualifies and its
+// window geometry, the kernel, the decide-and-copy kernel that finishes the
+// systems it converged, and the gate that opens the general sweep loop
+// (graph while node) only if some system is left.
+bool duo_plan(const MpArgs& p, int levels, DuoGeom* g);
+cudaError_t launch_mp_duo(const MpArgs& p, const DuoGeom& g, cudaStream_t s);
+cudaError_t launch_mp_duo_finish(const MpArgs& p, cudaStream_t s);
+cudaError_t launch_mp_gate(const MpArgs& p, cudaGraphConditionalHandle h, cudaStream_t s);
 cudaError_t launch_residual(const double* a, const double* b, const double* c, const double* d, const double* e,
                             const double* y, const double* x, double* r, int64_t m, int64_t n, int64_t ss,
                             int64_t rs, int64_t xss, int64_t xrs, cudaStream_t s);

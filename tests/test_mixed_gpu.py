@@ -318,3 +318,87 @@ def test_mixed_nan_input_reports_nonconvergence(cuda, n):
     for j in (0, 2):
         assert np.abs(x[j] - xg[j]).max() / np.abs(xg[j]).max() <= TOL
     assert np.isnan(x[1]).any()
+
+
+# --- sweeps 0 and 1 fused into one pass (mixed_duo.cu) ----------------------
+
+@pytest.mark.parametrize("kind,m,n", [(pcrp.GEN_DOMINANT, 4, 65536), (pcrp.GEN_WEAK, 2, 1 << 20),
+                                      (pcrp.GEN_DOMINANT, 3, 5002), (pcrp.GEN_WEAK, 5, 9000)])
+def test_mixed_fused_sweeps_match_general_kernels(cuda, kind, m, n, monkeypatch):
+    """Systems longer than one tile run their first two sweeps in one fused
+    pass (windows with halos, bulk-staged inputs, the factorisation kept in
+    tensor memory; PCRP_DUO=1); the general kernels solve the same systems:
+    both meet the bar, in two sweeps."""
+    arrs = pcrp.generate(kind, 23, m, n)
+    xg = O.ge(*arrs, m, n)
+    monkeypatch.setenv("PCRP_DUO", "1")
+    x, info, _ = run_mixed(arrs, m, n)
+    assert info.converged == 1 and info.sweeps == 2
+    assert O.fwd_err(x, xg, m, n) <= TOL
+    monkeypatch.delenv("PCRP_DUO")
+    xr, info_r, _ = run_mixed(arrs, m, n)
+    assert info_r.converged == 1
+    assert O.fwd_err(xr, xg, m, n) <= TOL
+
+
+def test_mixed_systems_left_by_fused_sweeps_run_the_general_kernels(cuda, monkeypatch):
+    """A tolerance that two sweeps cannot meet leaves every system to the
+    general kernels, which solve it from the start: the same bits as a solve
+    that never ran the fused pass, and more than two sweeps reported."""
+    import torch
+    m, n = 3, 20000
+    arrs = dd_bands(np.random.default_rng(41), m, n)
+    monkeypatch.setenv("PCRP_DUO", "1")
+    t = to_device(arrs, cuda)
+    pcrp.solve_mixed(*t, m, n, tol=1e-17, max_sweeps=4, report=False)
+    torch.cuda.synchronize()
+    fused = t[5].cpu().numpy()
+    monkeypatch.delenv("PCRP_DUO")
+    t2 = to_device(arrs, cuda)
+    pcrp.solve_mixed(*t2, m, n, tol=1e-17, max_sweeps=4, report=False)
+    torch.cuda.synchronize()
+    assert np.array_equal(fused.view(np.uint64), t2[5].cpu().numpy().view(np.uint64))
+    monkeypatch.setenv("PCRP_DUO", "1")
+    try:                       # (a correction that is exactly zero at the FP64 floor meets any tol)
+        _, info, _ = run_mixed(arrs, m, n, tol=1e-17, max_sweeps=4)
+        assert info.sweeps >= 3
+    except pcrp.PcrpError as ex:
+        assert ex.status == 5
+
+
+def test_mixed_fused_sweeps_bounded_wait_reports_timeout(cuda, monkeypatch):
+    """Failure detection without a fault: the test hook makes every CTA of
+    the fused kernel wait for a chunk that is never staged; the wait gives up
+    after ~4 ms, the general kernels still solve every system, the report
+    says PCRP_ETIMEOUT (status 4), and the context keeps working."""
+    m, n = 3, 65536
+    arrs = pcrp.generate(pcrp.GEN_DOMINANT, 29, m, n)
+    monkeypatch.setenv("PCRP_DUO", "1")
+    with pytest.raises(pcrp.PcrpError) as ei:
+        run_mixed(arrs, m, n, opts=pcrp.Opts(reserved0=0x7E57))
+    assert ei.value.status == 4
+    x, info, _ = run_mixed(arrs, m, n)
+    assert info.converged == 1 and O.fwd_err(x, O.ge(*arrs, m, n), m, n) <= TOL
+
+
+@pytest.mark.parametrize("n", [16384, 40000])
+def test_mixed_fused_sweeps_mixed_batch_and_nan(cuda, n, monkeypatch):
+    """Through the fused pass: a batch where dominant systems decouple and ADI
+    systems stay coupled (left to the general kernels), and a NaN in one
+    system's rhs that must surface as non-convergence while the others are
+    solved."""
+    monkeypatch.setenv("PCRP_DUO", "1")
+    dom = pcrp.generate(pcrp.GEN_DOMINANT, 3, 2, n)
+    adi = pcrp.generate(pcrp.GEN_ADI, 4, 2, n)
+    arrs = [np.concatenate([np.asarray(u), np.asarray(v)]) for u, v in zip(dom, adi)]
+    x, info, _ = run_mixed(arrs, 4, n, max_sweeps=16)
+    assert info.converged == 1
+    assert O.fwd_err(x[: 2 * n], O.ge(*dom, 2, n), 2, n) <= TOL
+    bad = [np.asarray(v).copy() for v in dom]
+    bad[5][n + n // 3] = np.nan
+    t = to_device(bad, cuda)
+    with pytest.raises(pcrp.PcrpError) as ei:
+        pcrp.solve_mixed(*t, 2, n, max_sweeps=4)
+    assert ei.value.status == 5
+    xs = t[5].cpu().numpy()
+    assert O.fwd_err(xs[:n], O.ge(*[v[:n] for v in bad], 1, n), 1, n) <= TOL
