@@ -269,44 +269,43 @@ __device__ __forceinline__ DuoTile duo_tile(const DuoGeom& g, int64_t j, int64_t
 // phases, so that a thread handles the same rows in both.
 __device__ __forceinline__ int tile_chunks(int64_t t0, int64_t t1) { return (int)((t1 - t0 + kDuoChunk - 1) / kDuoChunk); }
 
-// The producer's position in the CTA's stream of staged chunks.
-struct ChunkCursor {
-    TileWalk wk;
-    int64_t t0, t1;
-    int c, nch;
-};
-
-__device__ __forceinline__ void cursor_tile(ChunkCursor& q, const DuoGeom& g)
+// Staging of one chunk is split over six threads (lane 0 of warps 0..5),
+// one array each: each arms the slot's mbarrier with its own byte count
+// (the barrier expects six arrivals; a null outer band arrives with zero
+// bytes) and issues its bulk copy.  Chunk c of the tile at block rows
+// [t0, t1) of system j covers block rows t0 + c*kDuoChunk ...  The copies
+// ask L2 to keep the lines: the residual phase of this tile and the
+// neighbouring windows read them again.
+__device__ __forceinline__ void stage_array(const MpArgs& p, int a, int64_t j, int64_t t0, int64_t t1, int c,
+                                            double* slot_buf, uint64_t* bar)
 {
-    const int64_t wlo = q.wk.w * (int64_t)g.L, whi = min(wlo + (int64_t)g.L, g.nb);
-    q.t0 = max(wlo - (int64_t)g.H, (int64_t)0);
-    q.t1 = min(whi + (int64_t)g.H, g.nb);
-    q.c = 0;
-    q.nch = tile_chunks(q.t0, q.t1);
+    const double* src = a == 0 ? p.a : a == 1 ? p.b : a == 2 ? p.c : a == 3 ? p.d : a == 4 ? p.e : p.y;
+    const int64_t k0 = t0 + (int64_t)c * kDuoChunk;
+    const uint32_t bytes = src ? (uint32_t)(min((int64_t)kDuoChunk, t1 - k0) * 2 * sizeof(double)) : 0u;
+    mbar_expect_tx(bar, bytes);
+    if (src) bulk_g2s(slot_buf + a * 2 * kDuoChunk, src + j * p.n + 2 * k0, bytes, bar, policy_evict_last());
 }
 
-__device__ __forceinline__ void cursor_next(ChunkCursor& q, const DuoGeom& g, int64_t dj, int64_t dw)
+// Tile bounds [t0, t1) of window w.
+__device__ __forceinline__ void tile_span(const DuoGeom& g, int64_t w, int64_t& t0, int64_t& t1)
 {
-    if (++q.c < q.nch) return;
-    walk_next(q.wk, g, dj, dw);
-    cursor_tile(q, g);
+    const int64_t wlo = w * (int64_t)g.L, whi = min(wlo + (int64_t)g.L, g.nb);
+    t0 = max(wlo - (int64_t)g.H, (int64_t)0);
+    t1 = min(whi + (int64_t)g.H, g.nb);
 }
 
-// Thread 0: stage the cursor's chunk into a ring slot.  The copies ask L2 to
-// keep the lines: the residual phase of this tile and the neighbouring
-// windows read them again.
-__device__ __forceinline__ void stage_chunk(const MpArgs& p, const ChunkCursor& q, double* slot_buf, uint64_t* bar,
-                                            uint64_t pol)
+// Chunk cc counted from the start of tile (wn, [n0, n1)), resolved to the
+// tile that holds it (the last window of a system can be a single chunk);
+// wn.it >= items when the stream has ended.
+__device__ __forceinline__ void chunk_ahead(const DuoGeom& g, int64_t items, int64_t dj, int64_t dw, TileWalk& wn,
+                                            int64_t& n0, int64_t& n1, int& cc)
 {
-    const int64_t k0 = q.t0 + (int64_t)q.c * kDuoChunk;
-    const uint32_t bytes = (uint32_t)(min((int64_t)kDuoChunk, q.t1 - k0) * 2 * sizeof(double));
-    const double* src[kDuoArrays] = {p.a, p.b, p.c, p.d, p.e, p.y};
-    const uint32_t narr = 4u + (p.a ? 1u : 0u) + (p.e ? 1u : 0u);
-    mbar_expect_tx(bar, narr * bytes);
-    const int64_t off = q.wk.j * p.n + 2 * k0;
-#pragma unroll
-    for (int a = 0; a < kDuoArrays; a++)
-        if (src[a]) bulk_g2s(slot_buf + a * 2 * kDuoChunk, src[a] + off, bytes, bar, pol);
+    for (int nch = tile_chunks(n0, n1); cc >= nch; nch = tile_chunks(n0, n1)) {
+        cc -= nch;
+        walk_next(wn, g, dj, dw);
+        if (wn.it >= items) return;
+        tile_span(g, wn.w, n0, n1);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -488,12 +487,11 @@ mp_duo_kernel(MpArgs p, DuoGeom g)
     float2* sY = reinterpret_cast<float2*>(sU + kDuoRows);
     __shared__ __align__(8) uint64_t bars[kDuoSlots];
     __shared__ uint32_t tmem_base;
-    __shared__ ChunkCursor prod;                   // thread 0 (the producer): next chunk to stage
     __shared__ int64_t walk_dj, walk_dw;
 
     const int tid = threadIdx.x, bd = blockDim.x, h = tid & 1, r = tid >> 1, warp = tid >> 5;
     if (tid == 0) {
-        for (int s = 0; s < kDuoSlots; s++) mbar_init(&bars[s], 1);
+        for (int s = 0; s < kDuoSlots; s++) mbar_init(&bars[s], kDuoArrays);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         walk_dj = (int64_t)gridDim.x / g.nwin;
         walk_dw = (int64_t)gridDim.x - walk_dj * g.nwin;
@@ -511,16 +509,21 @@ mp_duo_kernel(MpArgs p, DuoGeom g)
     const int64_t items = p.m * g.nwin, n = p.n;
     const uint64_t limit = p.inject ? 4000000ull : 2000000000ull;   // ns
     const int64_t dj = walk_dj, dw = walk_dw;
+    // the stagers: lane 0 of warps 0..kDuoArrays-1, array `warp` each
+    const bool stager = (tid & 31) == 0 && warp < kDuoArrays;
     uint32_t issued = 0, used = 0;                 // chunks staged / consumed by this CTA
-    if (tid == 0) {
-        const uint64_t keep = policy_evict_last();
-        prod.wk = walk_start(g);
-        cursor_tile(prod, g);
-        for (int s = 0; s < kDuoSlots && prod.wk.it < items; s++) {
-            if (!(p.inject && issued == 0)) stage_chunk(p, prod, ring + s * kDuoSlotDoubles, &bars[s], keep);
-            issued++;
-            cursor_next(prod, g, dj, dw);
-        }
+    // the stream's first chunks
+    for (int s = 0; s < kDuoSlots; s++) {
+        TileWalk wn = walk_start(g);
+        if (wn.it >= items) break;
+        int64_t n0, n1;
+        tile_span(g, wn.w, n0, n1);
+        int cc = s;
+        chunk_ahead(g, items, dj, dw, wn, n0, n1, cc);
+        if (wn.it >= items) break;
+        if (stager && !(p.inject && issued == 0))
+            stage_array(p, warp, wn.j, n0, n1, cc, ring + s * kDuoSlotDoubles, &bars[s]);
+        issued++;
     }
     bool gave_up = false;
 
@@ -529,6 +532,10 @@ mp_duo_kernel(MpArgs p, DuoGeom g)
         const int TR = (int)(t.t1 - t.t0);
         const bool whole = t.t0 == 0 && t.t1 == g.nb;
         const int nch = tile_chunks(t.t0, t.t1);
+        // Band slots outside the system (n even): row i = 2kb+h has a_i, b_i
+        // unless kb = 0 (b_1 exists), d_i, e_i unless kb = nb-1 (d of the
+        // block row's first row exists); tile-local tests.
+        const bool sys_first = t.t0 == 0, sys_last = t.t1 == g.nb;
         // phase 0: the staged tile -> level-0 blocks with rhs y
         for (int c = 0; c < nch; c++, used++) {
             const int slot = (int)(used % kDuoSlots);
@@ -536,7 +543,7 @@ mp_duo_kernel(MpArgs p, DuoGeom g)
             if (__syncthreads_or(!got)) { gave_up = true; break; }
             const int k = c * kDuoChunk + r;
             const bool active = k < TR;
-            const int64_t i = 2 * (t.t0 + k) + h;
+            const bool at0 = sys_first && k == 0, atN = sys_last && k == TR - 1;
             const double* st = ring + slot * kDuoSlotDoubles + 2 * r + h;
             double a = 0.0, b = 0.0, cc = 1.0, d = 0.0, e = 0.0, y = 0.0;
             if (active) {
@@ -548,14 +555,23 @@ mp_duo_kernel(MpArgs p, DuoGeom g)
                 y = st[5 * 2 * kDuoChunk];
             }
             float mA, mB;
-            put_block_half(a, b, cc, d, e, y, i >= 2, i >= 1, i + 1 < n, i + 2 < n, h, active, k, sL, sU, sY, mA, mB);
+            put_block_half(a, b, cc, d, e, y, !at0, !(at0 && h == 0), !(atN && h == 1), !atN, h, active, k, sL, sU, sY,
+                           mA, mB);
             tmem_st2(tmab + 2u * c, mA, mB);        // (warp-uniform)
             __syncthreads();                       // the slot's data is consumed
-            if (tid == 0 && prod.wk.it < items) {
-                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                stage_chunk(p, prod, ring + slot * kDuoSlotDoubles, &bars[slot], policy_evict_last());
-                issued++;
-                cursor_next(prod, g, dj, dw);
+            // refill the slot with the chunk kDuoSlots ahead in the stream
+            {
+                TileWalk wn = wk;
+                int64_t n0 = t.t0, n1 = t.t1;
+                int cc = c + kDuoSlots;
+                chunk_ahead(g, items, dj, dw, wn, n0, n1, cc);
+                if (wn.it < items) {
+                    if (stager) {
+                        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                        stage_array(p, warp, wn.j, n0, n1, cc, ring + slot * kDuoSlotDoubles, &bars[slot]);
+                    }
+                    issued++;
+                }
             }
         }
         if (gave_up) break;
@@ -594,21 +610,21 @@ mp_duo_kernel(MpArgs p, DuoGeom g)
             const Row6 nxt = load_row6(p, rowbase + 2 * kn, c + 1 < nch && kn >= krl && kn < krh);
             float mA, mB;
             tmem_ld2(tmab + 2u * c, mA, mB);
-            const int64_t kb = t.t0 + k, i = 2 * kb + h;
             float rf = 0.0f;
             if (resid) {
+                const bool at0 = sys_first && k == 0, atN = sys_last && k == TR - 1;
                 // x_0 of rows i-2 .. i+2: tile rows k-1, k, k+1
                 const double2 xc = sX0[k];
-                const double2 xl = kb >= 1 ? sX0[k - 1] : make_double2(0.0, 0.0);
-                const double2 xr = 2 * kb + 2 < n ? sX0[k + 1] : make_double2(0.0, 0.0);
+                const double2 xl = !at0 ? sX0[k - 1] : make_double2(0.0, 0.0);
+                const double2 xr = !atN ? sX0[k + 1] : make_double2(0.0, 0.0);
                 const double xa = h ? xl.y : xl.x, xb = h ? xc.x : xl.y, xi = h ? xc.y : xc.x;
                 const double xd = h ? xr.x : xc.y, xe = h ? xr.y : xr.x;
                 // same FMA order as the refinement kernel of mixed.cu
                 double rhs = fma(-cur.c, xi, cur.y);
-                if (p.a && i >= 2) rhs = fma(-cur.a, xa, rhs);
-                if (i >= 1) rhs = fma(-cur.b, xb, rhs);
-                if (i + 1 < n) rhs = fma(-cur.d, xd, rhs);
-                if (p.e && i + 2 < n) rhs = fma(-cur.e, xe, rhs);
+                if (p.a && !at0) rhs = fma(-cur.a, xa, rhs);
+                if (!(at0 && h == 0)) rhs = fma(-cur.b, xb, rhs);
+                if (!(atN && h == 1)) rhs = fma(-cur.d, xd, rhs);
+                if (p.e && !atN) rhs = fma(-cur.e, xe, rhs);
                 rf = d2f_scaled(rhs, d_exponent(cur.c));
             }
             const float pf = __shfl_xor_sync(0xffffffffu, rf, 1);

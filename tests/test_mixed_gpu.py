@@ -323,7 +323,8 @@ def test_mixed_nan_input_reports_nonconvergence(cuda, n):
 # --- sweeps 0 and 1 fused into one pass (mixed_duo.cu) ----------------------
 
 @pytest.mark.parametrize("kind,m,n", [(pcrp.GEN_DOMINANT, 4, 65536), (pcrp.GEN_WEAK, 2, 1 << 20),
-                                      (pcrp.GEN_DOMINANT, 3, 5002), (pcrp.GEN_WEAK, 5, 9000)])
+                                      (pcrp.GEN_DOMINANT, 3, 5002), (pcrp.GEN_WEAK, 5, 9000),
+                                      (pcrp.GEN_DOMINANT, 3, 7682)])   # last window: one core block row
 def test_mixed_fused_sweeps_match_general_kernels(cuda, kind, m, n, monkeypatch):
     """Systems longer than one tile run their first two sweeps in one fused
     pass (windows with halos, bulk-staged inputs, the factorisation kept in
