@@ -52,6 +52,8 @@ MEASURED_TRAFFIC = {
     ("c1", "f64"): (495.4, "ncu capture m=48 n=65536, the 5 pcr_pass_kernel launches of one solve"),
     ("c1", "mixed"): (133.2, "ncu capture m=48 n=65536, mp_first_kernel + mp_try_kernel of one solve"),
     ("c2", "mixed"): (123.0, "ncu capture m=1024 n=4096, the mp_small_kernel launch of one solve"),
+    ("c4", "f64"): (517.0, "ncu capture m=4 n=2^20, the 5 pcr_pass_kernel launches of one solve"),
+    ("c4", "mixed"): (133.6, "ncu capture m=4 n=2^20, mp_first_kernel + mp_try_kernel of one solve"),
 }
 
 
@@ -410,6 +412,10 @@ def run_ours(args, world, rank, local, pg):
                              "reciprocal, so frac is the rate of the reference's operations, not the "
                              "FP64 pipe's busy share (ncu reports that)"}
 
+    # comparison legs (cuSPARSE, the other layout) time at most 5 solves: one
+    # cuSPARSE solve of the m=64 n=2^20 batch takes ~6 s
+    cmp_reps = min(max(3, args.steps), 5)
+
     # the other precision on the same inputs: FP32 PCR + FP64 refinement when the
     # headline is plain FP64 (and the reverse), for the mixed/FP64 speed ratio
     other = None
@@ -458,7 +464,7 @@ def run_ours(args, world, rank, local, pg):
         gbuf = torch.empty(max(1, int(nbytes.value)), dtype=torch.uint8, device=dev)
         gms = []
         with torch.cuda.stream(stream):
-            for it in range(max(3, args.steps) + 1):
+            for it in range(cmp_reps + 1):
                 for w, v in zip(work, inter):
                     w.copy_(v, non_blocking=True)
                 ek0.record(stream)
@@ -489,7 +495,7 @@ def run_ours(args, world, rank, local, pg):
             else (lambda: pcrp.solve_mixed(*alt, m, n, alt_lay, stream=stream, report=False, opts=opts))
         ams = []
         with torch.cuda.stream(stream):
-            for it in range(max(3, args.steps) + 1):
+            for it in range(cmp_reps + 1):
                 alt[5].copy_(alt_rhs, non_blocking=True)
                 if small:
                     flush.zero_()

@@ -9,9 +9,18 @@ runs the reference kernels with the reference's launch geometry
   <out>/cases.json              the cases with the sha256 of their inputs
   <out>/reference_outputs.npz   x of every case from both builds
 
+and, for the large cases (whole outputs would be tens of megabytes), per
+case the sha256 of each build's output bits, the per-system max |x|, the
+distances between the builds and to the FMA-free banded elimination
+(oracle), and row samples (the first, middle and last SAMPLE rows of every
+system) of both builds and of the elimination:
+
+  <out>/large_cases.json
+  <out>/large_samples.npz
+
 which are committed under tests/golden/.
 
-  python tests/golden/make_golden.py --out tests/golden
+  python tests/golden/make_golden.py --out tests/golden [--large-only]
 """
 import argparse
 import hashlib
@@ -43,6 +52,28 @@ CASES = [
 ]
 
 
+# (kind, seed, m, n, variant): the reference's splitting kernels hold up to
+# n = 2^19 (every stage-1 kernel looks one 512-row tile back)
+LARGE_CASES = [
+    (pcrp.GEN_DOMINANT, 201, 4, 16384, refrun.VARIANT_GLOBAL_SHARED),
+    (pcrp.GEN_ADI, 202, 4, 16384, refrun.VARIANT_GLOBAL_GLOBAL),
+    (pcrp.GEN_DOMINANT, 203, 4, 65536, refrun.VARIANT_GLOBAL_GLOBAL),
+    (pcrp.GEN_DOMINANT, 204, 4, 1 << 19, refrun.VARIANT_GLOBAL_SHARED),
+    (pcrp.GEN_WEAK, 205, 4, 1 << 19, refrun.VARIANT_GLOBAL_GLOBAL),
+]
+SAMPLE = 512
+
+
+def sample_rows(n: int) -> np.ndarray:
+    """Row indices of the samples kept for every system of a large case."""
+    mid = n // 2 - SAMPLE // 2
+    return np.concatenate([np.arange(SAMPLE), np.arange(mid, mid + SAMPLE), np.arange(n - SAMPLE, n)])
+
+
+def output_digest(x) -> str:
+    return hashlib.sha256(np.ascontiguousarray(x, dtype="<f8").tobytes()).hexdigest()
+
+
 def input_digest(arrs) -> str:
     h = hashlib.sha256()
     for v in arrs:
@@ -50,11 +81,38 @@ def input_digest(arrs) -> str:
     return h.hexdigest()
 
 
+def large(out_dir: str) -> None:
+    import oracle as O
+    manifest, samples = [], {}
+    for i, (kind, seed, m, n, variant) in enumerate(LARGE_CASES):
+        arrs = pcrp.generate(kind, seed, m, n)
+        xs = {b: refrun.solve(arrs, m, n, variant, fma=(b == "fma")) for b in ("nofma", "fma")}
+        xg = O.ge(*arrs, m, n)
+        rows = sample_rows(n)
+        entry = dict(case=i, kind=kind, seed=seed, m=m, n=n, variant=variant, inputs_sha256=input_digest(arrs),
+                     nofma_sha256=output_digest(xs["nofma"]), fma_sha256=output_digest(xs["fma"]),
+                     xmax=[float(np.abs(xs["nofma"][j * n:(j + 1) * n]).max()) for j in range(m)],
+                     fma_vs_nofma=O.fwd_err(xs["fma"], xs["nofma"], m, n),
+                     nofma_vs_ge=O.fwd_err(xs["nofma"], xg, m, n), fma_vs_ge=O.fwd_err(xs["fma"], xg, m, n))
+        for b, x in list(xs.items()) + [("ge", xg)]:
+            samples[f"large{i}_{b}"] = x.reshape(m, n)[:, rows].copy()
+        manifest.append(entry)
+        print(f"large case {i}: kind={kind} m={m} n={n} variant={variant}: fma vs nofma "
+              f"{entry['fma_vs_nofma']:.3e}, vs GE {entry['nofma_vs_ge']:.3e} / {entry['fma_vs_ge']:.3e}", flush=True)
+    with open(os.path.join(out_dir, "large_cases.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+    np.savez_compressed(os.path.join(out_dir, "large_samples.npz"), **samples)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.join(ROOT, "tests", "golden"))
+    ap.add_argument("--large-only", action="store_true", help="regenerate only the large cases")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
+    large(args.out)
+    if args.large_only:
+        return
     manifest, outs = [], {}
     for i, (kind, seed, m, n, variant) in enumerate(CASES):
         arrs = pcrp.generate(kind, seed, m, n)

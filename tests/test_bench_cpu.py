@@ -79,12 +79,16 @@ def dram_mb(path, names):
 # the ncu summaries the bench's traffic table was read from
 PROFILES = {("c1", "f64"): "profiles/pcr_pass_kernel_f64_m256_n65536.md",
             ("c1", "mixed"): "profiles/mixed_kernels_m256_n65536.md",
-            ("c2", "mixed"): "profiles/mixed_small_kernel_c2_m4096_n4096.md"}
+            ("c2", "mixed"): "profiles/mixed_small_kernel_c2_m4096_n4096.md",
+            ("c4", "f64"): "profiles/pcr_pass_kernel_f64_m64_n1048576.md",
+            ("c4", "mixed"): "profiles/mixed_kernels_m64_n1048576.md"}
 
 
 @pytest.mark.parametrize("key,col_names,units", [
     (("c1", "f64"), ["dram__bytes_read.sum (MB)", "dram__bytes_write.sum (MB)"], 48 * 65536),
     (("c1", "mixed"), ["dram__bytes_read.sum (MB)", "dram__bytes_write.sum (MB)"], 48 * 65536),
+    (("c4", "f64"), ["dram__bytes_read.sum (MB)", "dram__bytes_write.sum (MB)"], 4 << 20),
+    (("c4", "mixed"), ["dram__bytes_read.sum (MB)", "dram__bytes_write.sum (MB)"], 4 << 20),
 ])
 def test_measured_traffic_matches_profiles(key, col_names, units):
     """The bench's DRAM bytes per unknown equal the committed captures' sums."""
