@@ -1,19 +1,19 @@
 // tuned_params.h -- defaults chosen by the autotuner (pcrp/autotune.py) on NVIDIA GB300.
 // Regenerated by `python -m pcrp.autotune --write`; edit there, not here.
 #pragma once
-#define PCRP_TUNED_SMEM_ROWS 480     // ragged path: shared-memory capacity (rows)
+#define PCRP_TUNED_SMEM_ROWS 960     // ragged path: shared-memory capacity (rows)
 #define PCRP_TUNED_FUSE_STRIDES 3     // ragged path: strides fused per global pass
-#define PCRP_TUNED_TILE_ROWS 452      // ragged path: rows written per CTA in a global pass
-#define PCRP_TUNED_THREADS 128        // threads per CTA
+#define PCRP_TUNED_TILE_ROWS 932      // ragged path: rows written per CTA in a global pass
+#define PCRP_TUNED_THREADS 256        // threads per CTA
 #define PCRP_TUNED_MP_SMEM_BLOCKS 1024   // mixed: block rows solved whole in shared memory
 #define PCRP_TUNED_MP_FUSE 5            // mixed: FP32 block strides fused per global pass
 // FP64 path by system size: {n_max, smem_rows, fuse_strides, tile_rows, threads}
 #define PCRP_TUNED_F64_TABLE { \
-    {512, 960, 5, 836, 256}, \
-    {1024, 480, 3, 452, 128}, \
-    {8192, 960, 4, 900, 256}, \
+    {512, 1920, 2, 1908, 256}, \
+    {1024, 480, 4, 420, 128}, \
+    {8192, 960, 3, 932, 256}, \
     {131072, 480, 2, 468, 128}, \
-    {2097152, 480, 3, 452, 128} }
+    {2097152, 960, 3, 932, 256} }
 // mixed path by system size: {n_max, block rows in shared memory, fuse_strides}
 #define PCRP_TUNED_MP_TABLE { \
     {1024, 1024, 2}, \

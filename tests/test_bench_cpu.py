@@ -156,3 +156,27 @@ def test_reference_arm_does_not_load_libpcrp():
     out = subprocess.run([sys.executable, "-c", code], cwd=bench.ROOT, capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
     assert out.stdout.strip().splitlines()[-1] == "CLEAN"
+
+
+def test_tuned_params_header_is_the_autotuners_output():
+    """csrc/tuned_params.h is exactly what `python -m pcrp.autotune --write`
+    emits from the committed measurement record profiles/autotune_gb300.json."""
+    import json
+    sys.path.insert(0, os.path.join(bench.ROOT, "pcr-penta_gb300"))
+    from pcrp import autotune
+    with open(os.path.join(bench.ROOT, "profiles", "autotune_gb300.json")) as f:
+        rec = json.load(f)
+    with open(os.path.join(bench.ROOT, "pcr-penta_gb300", "csrc", "tuned_params.h")) as f:
+        assert f.read() == autotune.header_text(rec)
+
+
+def test_autotune_record_best_is_the_fastest_measured():
+    """Every size class's chosen plan is the fastest measurement of that class
+    in the committed record."""
+    import json
+    with open(os.path.join(bench.ROOT, "profiles", "autotune_gb300.json")) as f:
+        rec = json.load(f)
+    for kind in ("f64", "mixed"):
+        for b in rec[kind + "_best"]:
+            ms = [r["ms"] for r in rec[kind] if r["n"] == b["n"] and r["m"] == b["m"] and "ms" in r]
+            assert ms and b["ms"] == min(ms), (kind, b)
