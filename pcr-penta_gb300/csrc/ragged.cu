@@ -192,7 +192,13 @@ rg_persistent_kernel(RgArgs a)
             p.K = K[lvl]; p.final_step = fin ? 1 : 0; p.L = Lw[lvl]; p.H = H[lvl];
             p.nwin = nwin[lvl];
             p.TRmax = a.cap;
-            p.src_sub = 0; p.dst_sub = 0;             // ragged arrays keep the natural row order
+            // subsystem-major pass state, as in the uniform planner: each
+            // level's output groups every subsystem of the next level in one
+            // contiguous run of the system's rows, so later levels gather
+            // contiguously; the first level reads the caller's rows and the
+            // finish writes x in their natural order
+            p.src_sub = lvl > 0 ? 1 : 0;
+            p.dst_sub = fin ? 0 : 1;
             const int64_t r = fin ? i : i / nwin[lvl];
             const int64_t w = fin ? 0 : i - r * nwin[lvl];
             pcr_tile<kRgRPT, true>(p, k, r, w, smem);
