@@ -237,6 +237,15 @@ pcrp_status f64_solve(const double* a, const double* b, const double* c, const d
     const int64_t nrmax = ceil_div(n, p.G);
     p.K = ns - s1; p.H = 0; p.L = (int)nrmax; p.final_step = 1; p.nwin = 1;
     p.TRmax = (int)nrmax;
+    // whole systems read straight from the caller's arrays: bulk-staged
+    // tiles where every array row run is 16-byte aligned (contiguous layout,
+    // even n, aligned arrays)
+    if (s1 == 0 && layout == PCRP_LAYOUT_CONTIGUOUS && n % 2 == 0) {
+        bool aligned = true;
+        for (const double* q : {a, b, c, d, e, (const double*)y})
+            if (q && (reinterpret_cast<uintptr_t>(q) & 15)) aligned = false;
+        p.bulk = aligned ? 1 : 0;
+    }
     p.x = y; p.dst_ss = ss; p.dst_rs = rs; p.dst_sub = 0;
     for (int k = 0; k < NSTATE; k++) p.dst[k] = nullptr;
     cudaError_t ce = launch_pcr_pass(p, pl.threads, st, tri);

@@ -68,9 +68,12 @@
 #include "pcrp_internal.h"
 #include "mixed_internal.h"
 #include "mixed_dev.cuh"
+#include "tma.cuh"
 
 namespace pcrp {
 namespace {
+
+using namespace tma;
 
 constexpr int kDuoThreads = 512;                       // threads per CTA
 constexpr int kDuoRows = 1024;                         // block rows of a tile (two per thread at level 0)
@@ -96,63 +99,6 @@ static_assert(tmem_group_base(0) + 16 * tmem_group_levels(0) + 2 * kDuoMaxChunks
 static_assert(tmem_group_base(1) + 16 * tmem_group_levels(1) + 2 * kDuoMaxChunks <= tmem_group_base(2), "TMEM g1");
 static_assert(tmem_group_base(2) + 16 * tmem_group_levels(2) + 2 * kDuoMaxChunks <= tmem_group_base(3), "TMEM g2");
 // (warp group g reaches level l only if 128 g < 512 >> l: g = 1 up to l = 1, g = 2, 3 only l = 0)
-
-// ---------------------------------------------------------------------------
-// bulk asynchronous copies and mbarriers (inline PTX)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" :: "r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" :: "r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-                 : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ uint64_t global_ns()
-{
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
-    return t;
-}
-
-// Waits for phase `parity` of the barrier to complete; false after limit_ns.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
-{
-    if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = global_ns();
-    while (!mbar_try_wait(bar, parity))
-        if (global_ns() - t0 > limit_ns) return false;
-    return true;
-}
-
-__device__ __forceinline__ uint64_t policy_evict_last()
-{
-    uint64_t p;
-    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
-    return p;
-}
-
-// global -> shared bulk copy of `bytes` (multiple of 16, both addresses
-// 16-byte aligned), completing on `bar` (complete_tx), with an L2 policy.
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar, uint64_t pol)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
-                 "[%0], [%1], %2, [%3], %4;\n"
-                 :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol) : "memory");
-}
 
 // ---------------------------------------------------------------------------
 // tensor memory as per-thread scratch (inline PTX, tcgen05)
@@ -492,7 +438,7 @@ mp_duo_kernel(MpArgs p, DuoGeom g)
     const int tid = threadIdx.x, bd = blockDim.x, h = tid & 1, r = tid >> 1, warp = tid >> 5;
     if (tid == 0) {
         for (int s = 0; s < kDuoSlots; s++) mbar_init(&bars[s], kDuoArrays);
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        fence_mbarrier_init();
         walk_dj = (int64_t)gridDim.x / g.nwin;
         walk_dw = (int64_t)gridDim.x - walk_dj * g.nwin;
     }
@@ -567,7 +513,7 @@ mp_duo_kernel(MpArgs p, DuoGeom g)
                 chunk_ahead(g, items, dj, dw, wn, n0, n1, cc);
                 if (wn.it < items) {
                     if (stager) {
-                        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                        fence_proxy_async();
                         stage_array(p, warp, wn.j, n0, n1, cc, ring + slot * kDuoSlotDoubles, &bars[slot]);
                     }
                     issued++;

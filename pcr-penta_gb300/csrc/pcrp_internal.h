@@ -63,6 +63,8 @@ struct PcrPassArgs {
     int TRmax;                   // shared-memory rows per CTA (>= L + 2H, or whole subsystem)
     int src_sub;                 // 1: src is subsystem-major at stride G (uniform batches)
     int dst_sub;                 // 1: dst is subsystem-major at stride G*2^K (uniform batches)
+    int bulk;                    // 1: whole systems (G = 1, one tile) of even n in contiguous, 16-byte aligned
+                                 // arrays: the tile is staged by bulk asynchronous copies (one per array)
 };
 
 // Host-side launchers (pcr_f64.cu).  `tridiagonal`: the batch entered with

@@ -199,6 +199,7 @@ rg_persistent_kernel(RgArgs a)
             // finish writes x in their natural order
             p.src_sub = lvl > 0 ? 1 : 0;
             p.dst_sub = fin ? 0 : 1;
+            p.bulk = 0;                               // (per-thread loads through L2: data of this launch)
             const int64_t r = fin ? i : i / nwin[lvl];
             const int64_t w = fin ? 0 : i - r * nwin[lvl];
             pcr_tile<kRgRPT, true>(p, k, r, w, smem);
