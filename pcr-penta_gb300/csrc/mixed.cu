@@ -46,15 +46,35 @@ constexpr int kMpThreads = 256;
 constexpr int kMpTryThreads = 256;
 static_assert(kMpTile % kMpThreads == 0 && kMpThreads % 2 == 0, "refinement tiles: whole rows per thread, pairs in adjacent lanes");
 
-// x_s of rows [k0, k1) of system j (FP32 corrections d[k] of rows), with
-// the maxima of |dx| and |x| folded into dmax and xbits.
+// Row i of system j of an iterate: at j*ss + i*rs, or (ragged output, rg
+// non-null) at rg[j].x + i for i < rg[j].y; padding rows read as zero and
+// are not stored.
+__device__ __forceinline__ double x_read(const double* __restrict__ x, int64_t ss, int64_t rs,
+                                         const longlong2* __restrict__ rg, int64_t j, int64_t i)
+{
+    if (!rg) return x[j * ss + i * rs];
+    const longlong2 g = __ldg(rg + j);
+    return i < g.y ? x[g.x + i] : 0.0;
+}
+
+__device__ __forceinline__ void x_write(double* __restrict__ x, int64_t ss, int64_t rs,
+                                        const longlong2* __restrict__ rg, int64_t j, int64_t i, double v)
+{
+    if (!rg) { x[j * ss + i * rs] = v; return; }
+    const longlong2 g = __ldg(rg + j);
+    if (i < g.y) x[g.x + i] = v;
+}
+
+// x_s of row i of system j (FP32 correction d), with the maxima of |dx| and
+// |x| folded into dmax and xbits.
 __device__ __forceinline__ double x_update(const double* __restrict__ xsrc, int64_t xss, int64_t xrs,
-                                           double* __restrict__ xdst, int64_t dss, int64_t drs,
-                                           int64_t j, int64_t i, float d, float& dmax, unsigned long long& xbits)
+                                           const longlong2* srg, double* __restrict__ xdst, int64_t dss, int64_t drs,
+                                           const longlong2* drg, int64_t j, int64_t i, float d, float& dmax,
+                                           unsigned long long& xbits)
 {
     const double dd = f2d(d);
-    const double x = xsrc ? __dadd_rn(xsrc[j * xss + i * xrs], dd) : dd;
-    xdst[j * dss + i * drs] = x;
+    const double x = xsrc ? __dadd_rn(x_read(xsrc, xss, xrs, srg, j, i), dd) : dd;
+    x_write(xdst, dss, drs, drg, j, i, x);
     dmax = fmaxf(dmax, fabsf(d));
     xbits = max(xbits, absbits(x));
     return x;
@@ -62,17 +82,19 @@ __device__ __forceinline__ double x_update(const double* __restrict__ xsrc, int6
 
 // Iterates of sweep s: x_0 in X0 when more sweeps follow, every later x_s in
 // the output; x_{s-1} is read from where sweep s-1 wrote it.
-struct XView { const double* src; int64_t sss, srs; double* dst; int64_t dss, drs; };
+// The output of a ragged batch is addressed through rg.
+struct XView { const double* src; int64_t sss, srs; const longlong2* srg; double* dst; int64_t dss, drs; const longlong2* drg; };
 
 __device__ __forceinline__ XView x_view(int s, int max_sweeps, const double* X0, double* xout, int64_t n,
-                                        int64_t oss, int64_t ors)
+                                        int64_t oss, int64_t ors, const longlong2* rg)
 {
     XView v;
+    v.srg = nullptr; v.drg = nullptr;
     if (s == 0) { v.src = nullptr; v.sss = 0; v.srs = 0; }
     else if (s == 1) { v.src = X0; v.sss = n; v.srs = 1; }
-    else { v.src = xout; v.sss = oss; v.srs = ors; }
+    else { v.src = xout; v.sss = oss; v.srs = ors; v.srg = rg; }
     if (s == 0 && max_sweeps >= 2) { v.dst = const_cast<double*>(X0); v.dss = n; v.drs = 1; }
-    else { v.dst = xout; v.dss = oss; v.drs = ors; }
+    else { v.dst = xout; v.dss = oss; v.drs = ors; v.drg = rg; }
     return v;
 }
 
@@ -83,9 +105,9 @@ __device__ __forceinline__ void mp_resolve(MpArgs& p)
 {
     if (!p.ctr) return;
     p.sweep = *p.ctr;
-    const XView v = x_view(p.sweep, p.max_sweeps, p.X0, p.xout, p.n, p.oss, p.ors);
-    p.xsrc = v.src; p.xsrc_ss = v.sss; p.xsrc_rs = v.srs;
-    p.xdst = v.dst; p.xdst_ss = v.dss; p.xdst_rs = v.drs;
+    const XView v = x_view(p.sweep, p.max_sweeps, p.X0, p.xout, p.n, p.oss, p.ors, p.rg);
+    p.xsrc = v.src; p.xsrc_ss = v.sss; p.xsrc_rs = v.srs; p.xsrc_rg = v.srg;
+    p.xdst = v.dst; p.xdst_ss = v.dss; p.xdst_rs = v.drs; p.xdst_rg = v.drg;
 }
 
 __device__ __forceinline__ void mp_resolve(MpPassArgs& p)
@@ -102,22 +124,36 @@ __device__ __forceinline__ void mp_resolve(MpPassArgs& p)
     }
     if (p.nx0) {
         p.nx = p.nx0 + (size_t)s * p.m;
-        const XView v = x_view(s, p.max_sweeps, p.X0, p.xout, p.n, p.oss, p.ors);
-        p.xsrc = v.src; p.xsrc_ss = v.sss; p.xsrc_rs = v.srs;
-        p.xdst = v.dst; p.xdst_ss = v.dss; p.xdst_rs = v.drs;
+        const XView v = x_view(s, p.max_sweeps, p.X0, p.xout, p.n, p.oss, p.ors, p.rg);
+        p.xsrc = v.src; p.xsrc_ss = v.sss; p.xsrc_rs = v.srs; p.xsrc_rg = v.srg;
+        p.xdst = v.dst; p.xdst_ss = v.dss; p.xdst_rs = v.drs; p.xdst_rg = v.drg;
     }
 }
 
-// The six FP64 values of rows i0 = 2k and i1 = 2k+1 of one system (i1 may be
+// The six FP64 values of rows i0 = 2k and i1 = 2k+1 of system j (i1 may be
 // the dummy row n of an odd system).  Contiguous pairs at an even element
 // offset are read as one 16-byte load per array.  A null outer band (a or e)
-// is zero and not read.
+// is zero and not read.  In a ragged batch the rows past the system's own
+// are identity rows, and the band slots of its last rows that would couple
+// to them read as zero (the caller's values there are not part of the
+// system).
 struct PairRow { double a0, a1, b0, b1, c0, c1, d0, d1, e0, e1, y0, y1; };
 
-__device__ __forceinline__ PairRow load_pair(const MpArgs& p, int64_t base, int64_t i0)
+// RG: the batch is ragged (p.rg non-null); the uniform kernels are compiled
+// without the ragged addressing.
+template <bool RG>
+__device__ __forceinline__ PairRow load_pair(const MpArgs& p, int64_t j, int64_t i0)
 {
     PairRow P;
-    const int64_t n = p.n, rs = p.rs;
+    int64_t n = p.n, rs = p.rs, base = j * p.ss;
+    if (RG) {
+        const longlong2 g = __ldg(p.rg + j);
+        base = g.x; n = g.y; rs = 1;
+        if (i0 >= n) {
+            P = {0.0, 0.0, 0.0, 0.0, 1.0, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            return P;
+        }
+    }
     const int64_t g0 = base + i0 * rs;
     const double2 z = make_double2(0.0, 0.0);
     if (p.vec && rs == 1 && ((g0 & 1) == 0) && i0 + 1 < n) {
@@ -139,7 +175,31 @@ __device__ __forceinline__ PairRow load_pair(const MpArgs& p, int64_t base, int6
             P.a1 = 0.0; P.b1 = 0.0; P.c1 = 1.0; P.d1 = 0.0; P.e1 = 0.0; P.y1 = 0.0;
         }
     }
+    if (RG) {
+        if (i0 + 1 >= n) P.d0 = 0.0;
+        if (i0 + 2 >= n) { P.e0 = 0.0; P.d1 = 0.0; }
+        if (i0 + 3 >= n) P.e1 = 0.0;
+    }
     return P;
+}
+
+// Rows i0, i0+1 of the rhs of system j -> the contiguous copy Yc (zero on a
+// ragged system's padding rows).
+template <bool RG>
+__device__ __forceinline__ void copy_rhs_pair(const MpArgs& p, int64_t j, int64_t i0)
+{
+    const int64_t n = p.n;
+    double y0, y1 = 0.0;
+    if (RG) {
+        const longlong2 g = __ldg(p.rg + j);
+        y0 = i0 < g.y ? p.y[g.x + i0] : 0.0;
+        if (i0 + 1 < g.y) y1 = p.y[g.x + i0 + 1];
+    } else {
+        y0 = p.y[j * p.ss + i0 * p.rs];
+        if (i0 + 1 < n) y1 = p.y[j * p.ss + (i0 + 1) * p.rs];
+    }
+    p.Yc[j * n + i0] = y0;
+    if (i0 + 1 < n) p.Yc[j * n + i0 + 1] = y1;
 }
 
 // The FP32 row-scaled diagonal block and couplings of block row k (rows
@@ -180,9 +240,10 @@ __device__ __forceinline__ BlockRow block_of(const PairRow& P, int64_t i0, int64
 // the normalised couplings and rhs.
 struct PrepRow { M2 L, U, Mi; float2 Y; };
 
+template <bool RG>
 __device__ __forceinline__ PrepRow prep_row(const MpArgs& p, int64_t j, int64_t k)
 {
-    const PairRow P = load_pair(p, j * p.ss, 2 * k);
+    const PairRow P = load_pair<RG>(p, j, 2 * k);
     const BlockRow B = block_of(P, 2 * k, p.n);
     PrepRow r;
     r.Mi = minv(B.D);
@@ -220,6 +281,7 @@ mp_init_kernel(MpArgs p)
     if (t0 == 0 && p.err) *p.err = 0;
 }
 
+template <bool RG>
 __global__ void __launch_bounds__(kMpThreads)
 mp_prep_kernel(MpArgs p)
 {
@@ -229,10 +291,8 @@ mp_prep_kernel(MpArgs p)
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = q / nb, k = q - j * nb;
-        prep_store(p, q, prep_row(p, j, k));
-        const int64_t i0 = 2 * k;
-        p.Yc[j * p.n + i0] = p.y[j * p.ss + i0 * p.rs];
-        if (i0 + 1 < p.n) p.Yc[j * p.n + i0 + 1] = p.y[j * p.ss + (i0 + 1) * p.rs];
+        prep_store(p, q, prep_row<RG>(p, j, k));
+        copy_rhs_pair<RG>(p, j, 2 * k);
     }
     pdl_release();                                // (multi-wave grid: release once this CTA is done)
 }
@@ -457,9 +517,11 @@ __device__ __forceinline__ void try_solve(const MpPassArgs& p, const TryTile& t,
     for (int k = klo + threadIdx.x; k < khi; k += blockDim.x) {
         const int64_t i0 = 2 * (t.t0 + k);
         const float2 v = sY[swz(k)];
-        x_update(p.xsrc, p.xsrc_ss, p.xsrc_rs, p.xdst, p.xdst_ss, p.xdst_rs, t.j, i0, v.x, dmax, xbits);
+        x_update(p.xsrc, p.xsrc_ss, p.xsrc_rs, p.xsrc_rg, p.xdst, p.xdst_ss, p.xdst_rs, p.xdst_rg, t.j, i0, v.x,
+                 dmax, xbits);
         if (i0 + 1 < p.n)
-            x_update(p.xsrc, p.xsrc_ss, p.xsrc_rs, p.xdst, p.xdst_ss, p.xdst_rs, t.j, i0 + 1, v.y, dmax, xbits);
+            x_update(p.xsrc, p.xsrc_ss, p.xsrc_rs, p.xsrc_rg, p.xdst, p.xdst_ss, p.xdst_rs, p.xdst_rg, t.j, i0 + 1,
+                     v.y, dmax, xbits);
     }
     dmax = warp_max(dmax);
     const float xmax = warp_max(d2f_scaled(__longlong_as_double((long long)xbits), 0));
@@ -506,6 +568,7 @@ mp_try_kernel(MpPassArgs p)
 // No decision is needed in sweep 0, so nothing waits for other windows.  A
 // window whose system stays coupled marks it and stops after step 1; the
 // general passes and the refinement kernel then take the whole system.
+template <bool RG>
 __device__ __forceinline__ void first_item(const MpArgs& p, const MpWindows& g, int64_t item,
                                            float4* sL, float4* sU, float2* sY)
 {
@@ -519,14 +582,12 @@ __device__ __forceinline__ void first_item(const MpArgs& p, const MpWindows& g, 
 
     for (int k = tid; k < TR; k += bd) {
         const int64_t kb = t0 + k;
-        const PrepRow r = prep_row(p, j, kb);
+        const PrepRow r = prep_row<RG>(p, j, kb);
         const int sk = swz(k);
         sL[sk] = f4(r.L); sU[sk] = f4(r.U); sY[sk] = r.Y;
         if (kb >= wlo && kb < whi) {
             prep_store(p, j * nb + kb, r);
-            const int64_t i0 = 2 * kb;
-            p.Yc[j * n + i0] = p.y[j * p.ss + i0 * p.rs];
-            if (i0 + 1 < n) p.Yc[j * n + i0 + 1] = p.y[j * p.ss + (i0 + 1) * p.rs];
+            copy_rhs_pair<RG>(p, j, 2 * kb);
         }
     }
     __syncthreads();
@@ -571,7 +632,7 @@ __device__ __forceinline__ void first_item(const MpArgs& p, const MpWindows& g, 
     // refinement kernel), row-scaled and normalised -> the rhs of sweep 1
     for (int k = klo + tid; k < khi; k += bd) {
         const int64_t kb = t0 + k, i0 = 2 * kb;
-        const PairRow P = load_pair(p, j * p.ss, i0);
+        const PairRow P = load_pair<RG>(p, j, i0);
         const double2 xm = k > 0 ? sX[swz(k - 1)] : make_double2(0.0, 0.0);
         const double2 xc = sX[swz(k)];
         const double2 xp = k + 1 < TR ? sX[swz(k + 1)] : make_double2(0.0, 0.0);
@@ -600,6 +661,7 @@ __device__ __forceinline__ void first_item(const MpArgs& p, const MpWindows& g, 
 
 // Persistent CTAs over the windows of all systems (40 KB tiles of 1024
 // block rows, or whole systems of up to 2048), 4 per SM at most.
+template <bool RG>
 __global__ void __launch_bounds__(kMpTryThreads, 4)
 mp_first_kernel(MpArgs p, MpWindows g)
 {
@@ -614,7 +676,7 @@ mp_first_kernel(MpArgs p, MpWindows g)
     const int64_t items = p.m * g.nwin;
     for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
         if (__ldg(p.fin + it / g.nwin)) continue;   // finished by the fused first sweeps
-        first_item(p, g, it, sL, sU, sY);
+        first_item<RG>(p, g, it, sL, sU, sY);
         __syncthreads();
     }
 }
@@ -692,8 +754,8 @@ mp_xupdate_kernel(MpArgs p)
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const int64_t i = t0 + threadIdx.x + u * kMpThreads;
-            if (i < n) x_update(p.xsrc, p.xsrc_ss, p.xsrc_rs, p.xdst, p.xdst_ss, p.xdst_rs, j, i, p.dx[j * n + i],
-                                dmax, xbits);
+            if (i < n) x_update(p.xsrc, p.xsrc_ss, p.xsrc_rs, p.xsrc_rg, p.xdst, p.xdst_ss, p.xdst_rs, p.xdst_rg, j,
+                                i, p.dx[j * n + i], dmax, xbits);
         }
         float xmax = warp_max(d2f_scaled(__longlong_as_double((long long)xbits), 0));
         if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = xmax;
@@ -772,6 +834,7 @@ __device__ __forceinline__ void block_max(unsigned& dmb, unsigned long long& xb,
 
 constexpr int kMpSmallThreadsMax = 512;          // systems of >= 1024 block rows: 512 threads
 
+template <bool RG>
 __global__ void __launch_bounds__(kMpSmallThreadsMax, 2)
 mp_small_kernel(MpArgs p)
 {
@@ -789,7 +852,7 @@ mp_small_kernel(MpArgs p)
     for (int64_t j = blockIdx.x; j < p.m; j += gridDim.x) {
         double* __restrict__ X = p.X0 + j * n;
         for (int k = tid; k < TR; k += bd) {
-            const PrepRow r = prep_row(p, j, k);
+            const PrepRow r = prep_row<RG>(p, j, k);
             const int64_t q = j * nb + k;
             p.S0[2 * q] = f4(r.L);
             p.S0[2 * q + 1] = f4(r.U);
@@ -829,7 +892,7 @@ mp_small_kernel(MpArgs p)
             ndp = nd; nxp = nx;
             for (int k = tid; k < TR; k += bd) {
                 const int64_t i0 = 2 * (int64_t)k, q = j * nb + k;
-                const PairRow P = load_pair(p, j * p.ss, i0);
+                const PairRow P = load_pair<RG>(p, j, i0);
                 const double xm2 = i0 >= 2 ? X[i0 - 2] : 0.0, xm1 = i0 >= 1 ? X[i0 - 1] : 0.0, x0 = X[i0];
                 const double x1 = i0 + 1 < n ? X[i0 + 1] : 0.0, x2 = i0 + 2 < n ? X[i0 + 2] : 0.0;
                 const double x3 = i0 + 3 < n ? X[i0 + 3] : 0.0;
@@ -856,7 +919,7 @@ mp_small_kernel(MpArgs p)
             }
             __syncthreads();
         }
-        for (int64_t i = tid; i < n; i += bd) p.xout[j * p.oss + i * p.ors] = X[i];
+        for (int64_t i = tid; i < n; i += bd) x_write(p.xout, p.oss, p.ors, RG ? p.rg : nullptr, j, i, X[i]);
         if (tid == 0) { p.fin[j] = s + 1; p.status[j] = D.done ? 1 : 2; p.est[j] = D.est; }
         __syncthreads();                          // the next system reuses the tile
     }
@@ -866,8 +929,9 @@ mp_small_kernel(MpArgs p)
 // to FP32 by the power of two of the main diagonal; the odd row of a block
 // row reaches the even lane by a shuffle, which normalises the pair by the
 // block's diagonal inverse -> R[(s+1) & 1], the rhs of sweep s+1.
+template <bool RG>
 __device__ __forceinline__ void residual_tile(const MpArgs& p, int s, const double* __restrict__ x, int64_t xss,
-                                              int64_t xrs, int64_t j, int64_t tile, double* sx)
+                                              int64_t xrs, const longlong2* xrg, int64_t j, int64_t tile, double* sx)
 {
     const int tid = threadIdx.x;
     const int64_t n = p.n;
@@ -875,21 +939,28 @@ __device__ __forceinline__ void residual_tile(const MpArgs& p, int s, const doub
     const int64_t t0 = tile * kMpTile, t1 = min(t0 + kMpTile, n);
     const int64_t ih = tid < 2 ? t0 - 2 + tid : t1 + tid - 2;          // halo row of threads 0-3
     const bool halo = tid < 4 && ih >= 0 && ih < n;
-    const int64_t xs = j * xss;                           // x_s, written by this sweep's earlier kernels
+    // the system's rows in the caller arrays (a ragged system ends at nj <= n:
+    // identity rows beyond, and its slots coupling to them are zero)
+    int64_t base = j * p.ss, rs = p.rs, nj = n;
+    if (RG) { const longlong2 g = __ldg(p.rg + j); base = g.x; rs = 1; nj = g.y; }
+    else xrg = nullptr;
     double ba[XR], bb[XR], bc[XR], bd[XR], be[XR], by[XR];
 #pragma unroll
     for (int u = 0; u < XR; u++) {
         const int64_t i = t0 + tid + u * kMpThreads;
         ba[u] = 0.0; bb[u] = 0.0; bc[u] = 1.0; bd[u] = 0.0; be[u] = 0.0; by[u] = 0.0;
         if (i < t1) {
-            const int64_t g = j * p.ss + i * p.rs;
-            ba[u] = p.a ? p.a[g] : 0.0; bb[u] = p.b[g]; bc[u] = p.c[g]; bd[u] = p.d[g];
-            be[u] = p.e ? p.e[g] : 0.0;
+            if (i < nj) {
+                const int64_t g = base + i * rs;
+                ba[u] = p.a ? p.a[g] : 0.0; bb[u] = p.b[g]; bc[u] = p.c[g];
+                if (i + 1 < nj) bd[u] = p.d[g];
+                if (p.e && i + 2 < nj) be[u] = p.e[g];
+            }
             by[u] = p.Yc[j * n + i];
-            sx[tid + u * kMpThreads + 2] = x[xs + i * xrs];
+            sx[tid + u * kMpThreads + 2] = x_read(x, xss, xrs, xrg, j, i);
         }
     }
-    if (halo) sx[ih - t0 + 2] = x[xs + ih * xrs];
+    if (halo) sx[ih - t0 + 2] = x_read(x, xss, xrs, xrg, j, ih);
     __syncthreads();
 
     const int64_t nb = (n + 1) / 2;
@@ -928,6 +999,7 @@ __device__ __forceinline__ void residual_tile(const MpArgs& p, int s, const doub
 }
 
 // 5 CTAs per SM (at most 51 registers)
+template <bool RG>
 __global__ void __launch_bounds__(kMpThreads, 5)
 mp_residual_kernel(MpArgs p)
 {
@@ -938,9 +1010,10 @@ mp_residual_kernel(MpArgs p)
     const int s = p.ctr ? *p.ctr : p.sweep;
     const double* x = p.xdst;
     int64_t xss = p.xdst_ss, xrs = p.xdst_rs;
+    const longlong2* xrg = p.xdst_rg;
     if (p.ctr) {
-        const XView v = x_view(s, p.max_sweeps, p.X0, p.xout, p.n, p.oss, p.ors);
-        x = v.dst; xss = v.dss; xrs = v.drs;
+        const XView v = x_view(s, p.max_sweeps, p.X0, p.xout, p.n, p.oss, p.ors, p.rg);
+        x = v.dst; xss = v.dss; xrs = v.drs; xrg = v.drg;
     }
     if (__ldg(p.live + s + 1) == 0) return;       // every system has finished
     const bool fused0 = p.first_fused && s == 0;  // the fused sweep 0 formed r_0 of the systems it solved
@@ -950,7 +1023,7 @@ mp_residual_kernel(MpArgs p)
         const int64_t j = blk / tiles;
         if (__ldg(p.fin + j) != 0) continue;
         if (fused0 && !__ldg(p.fail + j)) continue;
-        residual_tile(p, s, x, xss, xrs, j, blk - j * tiles, sx);
+        residual_tile<RG>(p, s, x, xss, xrs, xrg, j, blk - j * tiles, sx);
         __syncthreads();
     }
 }
@@ -1064,11 +1137,12 @@ cudaError_t launch_mp_first(const MpArgs& p, const MpWindows& g, cudaStream_t s)
     const int64_t items = p.m * g.nwin;
     if (items <= 0) return cudaSuccess;
     const size_t smem = mp_pass_smem(g.TRmax);
-    cudaError_t e = cudaFuncSetAttribute(mp_first_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    auto kern = p.rg ? mp_first_kernel<true> : mp_first_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)mp_pass_smem(kMpMaxRows));
     if (e != cudaSuccess) return e;
-    const int64_t blocks = std::min<int64_t>(items, mp_grid_cap((const void*)mp_first_kernel, kMpTryThreads, smem));
-    e = launch_dependent(mp_first_kernel, (unsigned)blocks, kMpTryThreads, smem, s, p, g);
+    const int64_t blocks = std::min<int64_t>(items, mp_grid_cap((const void*)kern, kMpTryThreads, smem));
+    e = launch_dependent(kern, (unsigned)blocks, kMpTryThreads, smem, s, p, g);
     count_launch();
     return e;
 }
@@ -1077,7 +1151,8 @@ cudaError_t launch_mp_prep(const MpArgs& p, cudaStream_t s)
 {
     const int64_t nb = (p.n + 1) / 2;
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>((p.m * nb + kMpThreads - 1) / kMpThreads, 152 * 16));
-    const cudaError_t e = launch_dependent(mp_prep_kernel, (unsigned)blocks, kMpThreads, 0, s, p);
+    const cudaError_t e = launch_dependent(p.rg ? mp_prep_kernel<true> : mp_prep_kernel<false>, (unsigned)blocks,
+                                           kMpThreads, 0, s, p);
     count_launch();
     return e;
 }
@@ -1119,7 +1194,8 @@ cudaError_t launch_mp_small(const MpArgs& p, cudaStream_t s)
     if (nb > kMpMaxRows) return cudaErrorInvalidValue;
     if (p.m <= 0) return cudaSuccess;
     const size_t smem = mp_pass_smem((int)nb);
-    cudaError_t e = cudaFuncSetAttribute(mp_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    auto kern = p.rg ? mp_small_kernel<true> : mp_small_kernel<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)mp_pass_smem(kMpMaxRows));
     if (e != cudaSuccess) return e;
     // large tiles hold two CTAs per SM (shared memory): twice the threads per
@@ -1128,8 +1204,8 @@ cudaError_t launch_mp_small(const MpArgs& p, cudaStream_t s)
     // so small systems fill the SM with more CTAs instead of idle threads
     const int threads = nb >= 1024 ? kMpSmallThreadsMax
                         : nb >= kMpThreads ? kMpThreads : (int)std::max<int64_t>(32, (nb + 31) / 32 * 32);
-    const int64_t blocks = std::min<int64_t>(p.m, mp_grid_cap((const void*)mp_small_kernel, threads, smem));
-    e = launch_dependent(mp_small_kernel, (unsigned)blocks, threads, smem, s, p);
+    const int64_t blocks = std::min<int64_t>(p.m, mp_grid_cap((const void*)kern, threads, smem));
+    e = launch_dependent(kern, (unsigned)blocks, threads, smem, s, p);
     count_launch();
     return e;
 }
@@ -1156,8 +1232,9 @@ cudaError_t launch_mp_residual(const MpArgs& p, cudaStream_t s)
     // one wave of CTAs striding over the tiles: a sweep after which every
     // system has finished returns at once through the live count
     const int64_t tiles = (p.n + kMpTile - 1) / kMpTile;
-    const int64_t blocks = std::min<int64_t>(p.m * tiles, mp_grid_cap((const void*)mp_residual_kernel, kMpThreads, 0));
-    const cudaError_t e = launch_dependent(mp_residual_kernel, (unsigned)blocks, kMpThreads, 0, s, p);
+    auto kern = p.rg ? mp_residual_kernel<true> : mp_residual_kernel<false>;
+    const int64_t blocks = std::min<int64_t>(p.m * tiles, mp_grid_cap((const void*)kern, kMpThreads, 0));
+    const cudaError_t e = launch_dependent(kern, (unsigned)blocks, kMpThreads, 0, s, p);
     count_launch();
     return e;
 }

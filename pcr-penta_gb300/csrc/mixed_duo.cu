@@ -660,7 +660,7 @@ bool duo_plan(const MpArgs& p, int levels, DuoGeom* g)
     // contiguous systems of even n, 16-byte aligned arrays (whole 16-byte
     // row pairs for the bulk copies), at least two sweeps, and windows that
     // leave a core
-    if (levels < 1 || levels > kDuoMaxLevels || p.max_sweeps < 2 || !p.vec) return false;
+    if (levels < 1 || levels > kDuoMaxLevels || p.max_sweeps < 2 || !p.vec || p.rg) return false;
     if (p.rs != 1 || p.ss != p.n || (p.n & 1) || p.xout == nullptr || p.ors != 1 || p.oss != p.n) return false;
     if (reinterpret_cast<uintptr_t>(p.X0) & 15 || reinterpret_cast<uintptr_t>(p.xout) & 15) return false;
     // Opt-in (PCRP_DUO=1) while the fused pass is slower than the general

@@ -112,11 +112,12 @@ pcrp_status enqueue_sweep(MpArgs A, const SweepPlan& S, int s, cudaStream_t st)
     cudaError_t ce;
     if (!dev) {
         A.sweep = s;
+        A.xsrc_rg = nullptr; A.xdst_rg = nullptr;
         if (s == 0) { A.xsrc = nullptr; A.xsrc_ss = 0; A.xsrc_rs = 0; }
         else if (s == 1) { A.xsrc = A.X0; A.xsrc_ss = n; A.xsrc_rs = 1; }
-        else { A.xsrc = A.xout; A.xsrc_ss = A.oss; A.xsrc_rs = A.ors; }
+        else { A.xsrc = A.xout; A.xsrc_ss = A.oss; A.xsrc_rs = A.ors; A.xsrc_rg = A.rg; }
         if (s == 0 && A.max_sweeps >= 2) { A.xdst = A.X0; A.xdst_ss = n; A.xdst_rs = 1; }
-        else { A.xdst = A.xout; A.xdst_ss = A.oss; A.xdst_rs = A.ors; }
+        else { A.xdst = A.xout; A.xdst_ss = A.oss; A.xdst_rs = A.ors; A.xdst_rg = A.rg; }
     }
 
     // FP32 block solve of the normalised system with rhs R[s & 1]
@@ -126,7 +127,7 @@ pcrp_status enqueue_sweep(MpArgs A, const SweepPlan& S, int s, cudaStream_t st)
     p.m = m; p.n = n; p.nb = nb; p.G = 1;
     if (dev) {
         p.ctr = A.ctr; p.live0 = A.live; p.R0 = A.R[0]; p.R1 = A.R[1]; p.pre0 = A.ndx_pre;
-        p.X0 = A.X0; p.xout = A.xout; p.oss = A.oss; p.ors = A.ors; p.max_sweeps = A.max_sweeps;
+        p.X0 = A.X0; p.xout = A.xout; p.oss = A.oss; p.ors = A.ors; p.rg = A.rg; p.max_sweeps = A.max_sweeps;
     } else {
         p.sweep = s; p.srcY = A.R[s & 1]; p.live = A.live + s;
     }
@@ -141,8 +142,8 @@ pcrp_status enqueue_sweep(MpArgs A, const SweepPlan& S, int s, cudaStream_t st)
         if (dev) {
             t.pre0 = nullptr; t.level0 = 1; t.nx0 = A.nx; t.skip0 = S.fused;
         } else {
-            t.xsrc = A.xsrc; t.xsrc_ss = A.xsrc_ss; t.xsrc_rs = A.xsrc_rs;
-            t.xdst = A.xdst; t.xdst_ss = A.xdst_ss; t.xdst_rs = A.xdst_rs;
+            t.xsrc = A.xsrc; t.xsrc_ss = A.xsrc_ss; t.xsrc_rs = A.xsrc_rs; t.xsrc_rg = A.xsrc_rg;
+            t.xdst = A.xdst; t.xdst_ss = A.xdst_ss; t.xdst_rs = A.xdst_rs; t.xdst_rg = A.xdst_rg;
             t.nx = A.nx + (size_t)s * m;
         }
         ce = launch_mp_try(t, st);
@@ -207,7 +208,7 @@ pcrp_status enqueue_sweep(MpArgs A, const SweepPlan& S, int s, cudaStream_t st)
 // ---------------------------------------------------------------------------
 struct GraphKey {
     int dev;
-    const void* ptr[8];
+    const void* ptr[9];
     int64_t m, n, ss, rs;
     double tol;
     int max_sweeps, cap, fuse, win, duo;
@@ -319,8 +320,8 @@ pcrp_status launch_sweep_graph(const MpArgs& A, const SweepPlan& S, cudaStream_t
     GraphKey k;
     std::memset(&k, 0, sizeof k);
     if (cudaGetDevice(&k.dev) != cudaSuccess) return PCRP_ENOTSUP;
-    const void* ptrs[8] = {A.a, A.b, A.c, A.d, A.e, A.y, A.S0, A.xout};
-    for (int i = 0; i < 8; i++) k.ptr[i] = ptrs[i];
+    const void* ptrs[9] = {A.a, A.b, A.c, A.d, A.e, A.y, A.S0, A.xout, A.rg};
+    for (int i = 0; i < 9; i++) k.ptr[i] = ptrs[i];
     k.m = A.m; k.n = A.n; k.ss = A.ss; k.rs = A.rs; k.tol = A.tol; k.max_sweeps = A.max_sweeps;
     k.cap = S.pl.cap; k.fuse = S.pl.fuse; k.win = S.pl.win; k.duo = S.duo;
     std::lock_guard<std::mutex> lk(g_graph_mu);
@@ -370,7 +371,7 @@ size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_s
 pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, const double* d, const double* e,
                           double* y, int64_t m, int64_t n, int64_t ss, int64_t rs, double tol, int max_sweeps,
                           const pcrp_opts* opts, bool keep_x, void* ws, cudaStream_t st, MpArgs* out,
-                          const MixedDest* dest, bool* dest_written)
+                          const MixedDest* dest, bool* dest_written, const longlong2* rg)
 {
     const char* who = "pcrp_solve_mixed";
     if (dest_written) *dest_written = false;
@@ -384,7 +385,11 @@ pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, con
 
     MpArgs A{};
     A.a = a; A.b = b; A.c = c; A.d = d; A.e = e; A.y = y;
-    A.m = m; A.n = n; A.ss = ss; A.rs = rs;
+    if (rg) {                                    // a ragged batch keeps no report and has no adapter
+        if (keep_x || dest) return set_error(PCRP_EINVAL, "%s: internal: ragged batch with a report", who);
+        ss = n; rs = 1;
+    }
+    A.m = m; A.n = n; A.ss = ss; A.rs = rs; A.rg = rg;
     A.S0 = reinterpret_cast<float4*>(base + WL.S0);
     A.R[0] = reinterpret_cast<float2*>(base + WL.R);
     A.R[1] = A.R[0] + T;

@@ -18,6 +18,10 @@ struct MpArgs {
     const double *a, *b, *c, *d, *e;   // caller bands, layout (ss, rs)
     double* y;                          // caller rhs in, solution out
     int64_t m, n, ss, rs;
+    const longlong2* rg;                // ragged batch: system j is rows rg[j].x .. rg[j].x + rg[j].y - 1 of
+                                        // the caller arrays (row stride 1) and rows rg[j].y .. n-1 are identity
+                                        // padding (zero rhs, zero couplings) that is neither read nor written
+                                        // there; null: uniform batch addressed by (ss, rs)
     float4* S0;                         // level-0 normalised L,U: [2*q] = L, [2*q+1] = U, q < m*nb
     float2* R[2];                       // normalised rhs Y of block row q: sweep s reads R[s & 1]
     float4* Mi;                         // inverse of the row-scaled FP32 diagonal block of block row q
@@ -27,8 +31,10 @@ struct MpArgs {
     double* Yc;                         // copy of the rhs, m*n contiguous (y may hold the iterate)
     const double* xsrc;                 // this sweep's x_{s-1} (null in sweep 0) ...
     int64_t xsrc_ss, xsrc_rs;           //   ... and its system / row strides
+    const longlong2* xsrc_rg;           //   ... or its ragged rows (rg, when xsrc is the output)
     double* xdst;                       // this sweep's x_s ...
     int64_t xdst_ss, xdst_rs;
+    const longlong2* xdst_rg;
     double* xout;                       // the output iterate (y or Xout) and its strides: x_s of sweeps >= 1
     int64_t oss, ors;
     int* ctr;                           // device sweep counter (graph-driven sweeps), or null: `sweep` and the
@@ -73,8 +79,10 @@ struct MpPassArgs {
     int* nfail;                         // number of systems with fail set
     const double* xsrc;                 // cyclic-reduction passes: x_{s-1} (null in sweep 0) ...
     int64_t xsrc_ss, xsrc_rs;
+    const longlong2* xsrc_rg;
     double* xdst;                       //   ... and x_s = x_{s-1} + dx_s (null: write dx instead)
     int64_t xdst_ss, xdst_rs;
+    const longlong2* xdst_rg;
     unsigned* nx;                       //   ... and max |x_s|
     // Graph-driven sweeps: the fields above that change from sweep to sweep
     // (sweep, live, srcY at level 0, ndx_pre_in/out, xsrc, xdst, nx) are
@@ -88,6 +96,7 @@ struct MpPassArgs {
     const double* X0;
     double* xout;
     int64_t oss, ors;
+    const longlong2* rg;                // ragged output rows (see MpArgs::rg)
     int pass, max_sweeps, level0, skip0;   // skip0: sweep 0 belongs to the fused kernel
     int64_t m, n, nb, G, nwin;
     int K, final_step, L, H, TRmax, sweep;
@@ -142,10 +151,14 @@ struct MixedDest {
 // Enqueues a uniform batch on `st` (mixed_host.cpp).  With `dest`, a solve of
 // whole systems that keeps no report writes x to *dest and sets
 // *dest_written; any other solve ignores it.
+// With `rg` (device array of m (offset, rows) pairs, every rows <= n), the
+// batch is m ragged systems of the caller arrays solved as n-row systems
+// (see MpArgs::rg); ss and rs are then ignored.
 pcrp_status mixed_enqueue(const double* a, const double* b, const double* c, const double* d, const double* e,
                           double* y, int64_t m, int64_t n, int64_t ss, int64_t rs, double tol, int max_sweeps,
                           const pcrp_opts* opts, bool keep_x, void* ws, cudaStream_t st, MpArgs* out,
-                          const MixedDest* dest = nullptr, bool* dest_written = nullptr);
+                          const MixedDest* dest = nullptr, bool* dest_written = nullptr,
+                          const longlong2* rg = nullptr);
 
 cudaError_t launch_mp_init(const MpArgs& p, cudaStream_t s);
 cudaError_t launch_mp_first(const MpArgs& p, const MpWindows& g, cudaStream_t s);

@@ -1,15 +1,19 @@
 // ragged_mixed.cu -- mixed-precision mode of pcrp_solve_ragged.
 //
-// Systems are binned by size into power-of-two classes N (n in (N/2, N]).
-// Each class is gathered into a uniform padded batch (rows n..N-1 are
-// identity rows with zero right-hand side, and the couplings that would reach
-// them -- the out-of-range slots d_{n-1}, e_{n-2}, e_{n-1} -- are zeroed), so
-// the padded solution restricted to the first n rows is the system's own.
-// Each class runs the uniform mixed-precision solver (FP32 block reduction +
-// FP64 refinement, its sweep loop a while node that stops at convergence),
-// then the solutions are scattered back.  The classes are independent
-// branches of one CUDA graph, captured once per (pointers, sizes) and
-// replayed.
+// Systems are binned by size into classes N a quarter of an octave apart
+// (n in (2^k, 2^(k+1)] rounds up to a multiple of 2^(k-2): N/2^k is 5/4,
+// 6/4, 7/4 or 2).  Each class runs the uniform mixed-precision solver (FP32
+// block reduction + FP64 refinement, its sweep loop a while node that stops
+// at convergence) as a batch of N-row systems that reads and writes the
+// caller's arrays in place through a table of (first row, rows) per system:
+// rows n..N-1 of a system are identity rows with zero right-hand side that
+// exist only in the solver's own workspace, and the band slots that would
+// couple the system to them (d_{n-1}, e_{n-2}, e_{n-1}) read as zero, so the
+// padded solution restricted to the first n rows is the system's own.
+// Padding adds at most a quarter and about an eighth of the rows on average
+// to the solver's work, and nothing to the traffic on the caller's arrays.
+// The classes are independent branches of one CUDA graph, captured once per
+// (pointers, sizes) and replayed.
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -26,54 +30,45 @@ size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_s
 
 namespace {
 
-__global__ void rgm_gather_kernel(const double* __restrict__ a, const double* __restrict__ b,
-                                  const double* __restrict__ c, const double* __restrict__ d,
-                                  const double* __restrict__ e, const double* __restrict__ y,
-                                  const int64_t* __restrict__ offsets, const int64_t* __restrict__ sys,
-                                  int64_t ms, int64_t N, double* __restrict__ out)
+// (first row, rows) of the systems of every class, class after class, from
+// the offsets: the table the solver addresses the caller arrays through
+__global__ void rgm_rows_kernel(const int64_t* __restrict__ offsets, const int64_t* __restrict__ sys, int64_t cnt,
+                                longlong2* __restrict__ rows)
 {
-    const int64_t total = ms * N;
-    double* pa = out; double* pb = pa + total; double* pc = pb + total;
-    double* pd = pc + total; double* pe = pd + total; double* py = pe + total;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t s = q / N, i = q - s * N;
-        const int64_t k = sys[s];
-        const int64_t o = offsets[k], n = offsets[k + 1] - o;
-        if (i < n) {
-            pa[q] = (a && i >= 2) ? a[o + i] : 0.0;             // a null outer band is zero
-            pb[q] = i >= 1 ? b[o + i] : 0.0;
-            pc[q] = c[o + i];
-            pd[q] = i + 1 < n ? d[o + i] : 0.0;
-            pe[q] = (e && i + 2 < n) ? e[o + i] : 0.0;
-            py[q] = y[o + i];
-        } else {
-            pa[q] = 0.0; pb[q] = 0.0; pc[q] = 1.0; pd[q] = 0.0; pe[q] = 0.0; py[q] = 0.0;
-        }
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < cnt; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = sys[q];
+        const int64_t o = offsets[k];
+        rows[q] = make_longlong2(o, offsets[k + 1] - o);
     }
 }
 
-__global__ void rgm_scatter_kernel(const double* __restrict__ px, const int64_t* __restrict__ offsets,
-                                   const int64_t* __restrict__ sys, int64_t ms, int64_t N, double* __restrict__ y,
-                                   const int* __restrict__ status, int* __restrict__ unconverged)
+// systems of a class that did not converge (status 1: converged)
+__global__ void rgm_count_kernel(const int* __restrict__ status, int64_t ms, int* __restrict__ unconverged)
 {
-    const int64_t total = ms * N;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t s = q / N, i = q - s * N;
-        const int64_t k = sys[s];
-        const int64_t o = offsets[k], n = offsets[k + 1] - o;
-        if (i < n) y[o + i] = px[q];
-        if (i == 0 && status[s] != 1) atomicAdd(unconverged, 1);
-    }
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < ms; j += (int64_t)gridDim.x * blockDim.x)
+        if (status[j] != 1) atomicAdd(unconverged, 1);
+}
+
+// The padded size of a system of n rows: n rounded up to a multiple of a
+// quarter of its octave (2^(k-2) for n in (2^k, 2^(k+1)]), at least 2.
+int64_t size_class(int64_t n)
+{
+    if (n <= 2) return 2;
+    int k = 0;
+    while ((int64_t(1) << (k + 1)) < n) k++;        // 2^k < n <= 2^(k+1)
+    const int64_t step = int64_t(1) << std::max(k - 2, 0);
+    return (n + step - 1) / step * step;
 }
 
 unsigned grid_for(int64_t total) {
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152 * 16));
 }
 
+// A batch: its pointers, stream, sizes (hashed) and solver settings.
 struct Key {
     int dev;
     cudaStream_t s;
-    const void* p[8];
+    const void* p[7];
     int64_t nsys;
     uint64_t hash;
     double tol;
@@ -81,15 +76,29 @@ struct Key {
     bool operator<(const Key& o) const {
         if (dev != o.dev) return dev < o.dev;
         if (s != o.s) return s < o.s;
-        for (int q = 0; q < 8; q++) if (p[q] != o.p[q]) return p[q] < o.p[q];
+        for (int q = 0; q < 7; q++) if (p[q] != o.p[q]) return p[q] < o.p[q];
         if (nsys != o.nsys) return nsys < o.nsys;
         if (hash != o.hash) return hash < o.hash;
         if (tol != o.tol) return tol < o.tol;
         return sweeps < o.sweeps;
     }
 };
+
+// The batch's graph, the workspace it was captured on, and the device list
+// of system indices (class after class) it reads; everything per call is in
+// the graph, so a replay needs no upload.
+struct Entry {
+    size_t total = 0;                 // workspace bytes
+    void* ws = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t kernels = 0;
+    int64_t* d_sys = nullptr;
+    uint64_t used = 0;
+};
 std::mutex g_mu;
-std::map<Key, std::pair<cudaGraphExec_t, int64_t>> g_exec;   // graph and its kernel count
+std::map<Key, Entry> g_exec;
+uint64_t g_clock = 0;
+constexpr size_t kMaxEntries = 16;               // batches remembered (least recently used dropped)
 
 }  // namespace
 
@@ -110,9 +119,6 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
     if (ce != cudaSuccess) return cuda_error(ce, "pcrp_solve_ragged: reading offsets");
     if (off[0] != 0) return set_error(PCRP_EINVAL, "pcrp_solve_ragged: offsets[0] = %lld, expected 0", (long long)off[0]);
-
-    // size classes
-    std::map<int64_t, std::vector<int64_t>> cls;
     uint64_t h = 1469598103934665603ULL;
     for (int64_t k = 0; k < nsys; k++) {
         const int64_t n = off[k + 1] - off[k];
@@ -120,64 +126,105 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
             return set_error(PCRP_EINVAL, "pcrp_solve_ragged: system %lld has %lld rows (max_rows %lld)",
                              (long long)k, (long long)n, (long long)max_rows);
         h = (h ^ (uint64_t)n) * 1099511628211ULL;
-        if (n == 0) continue;
-        int64_t N = 2;
-        while (N < n) N <<= 1;
-        cls[N].push_back(k);
     }
-    // workspace: [system lists | counter | per class: padded batch, mixed scratch]
-    // (every class has its own, so that the classes run concurrently)
-    auto r256 = [](size_t v) { return (v + 255) / 256 * 256; };
-    std::vector<size_t> pad_off, mix_off;
-    size_t per_class = 0;
-    for (auto& kv : cls) {
-        const int64_t ms = (int64_t)kv.second.size(), N = kv.first;
-        pad_off.push_back(per_class);
-        per_class += r256((size_t)6 * ms * N * sizeof(double));
-        mix_off.push_back(per_class);
-        per_class += r256(mixed_workspace_bytes(ms, N, o, max_sweeps, false, PCRP_LAYOUT_CONTIGUOUS));
-    }
-    const size_t lists = r256((size_t)nsys * sizeof(int64_t));
-    const size_t total = lists + 256 + per_class;
-    void* ws = nullptr;
-    pcrp_status rc = get_workspace(o, total, st, &ws);
-    if (rc != PCRP_OK) return rc;
-    char* base = static_cast<char*>(ws);
-    int64_t* d_lists = reinterpret_cast<int64_t*>(base);
-    int* d_unconv = reinterpret_cast<int*>(base + lists);
-    char* d_class = base + lists + 256;
-
-    std::vector<int64_t> h_lists;
-    h_lists.reserve(nsys);
-    for (auto& kv : cls) h_lists.insert(h_lists.end(), kv.second.begin(), kv.second.end());
 
     int dev = 0;
     ce = cudaGetDevice(&dev);
     if (ce != cudaSuccess) return cuda_error(ce, "cudaGetDevice");
     Key key{};
     key.dev = dev; key.s = st;
-    const void* ptrs[8] = {a, b, c, d, e, y, offsets, ws};
-    for (int q = 0; q < 8; q++) key.p[q] = ptrs[q];
+    const void* ptrs[7] = {a, b, c, d, e, y, offsets};
+    for (int q = 0; q < 7; q++) key.p[q] = ptrs[q];
     key.nsys = nsys; key.hash = h; key.tol = tol; key.sweeps = max_sweeps;
 
-    // the system lists are not graph nodes (they change with the offsets' content, which the key hashes)
-    if (!h_lists.empty()) {
-        ce = cudaMemcpyAsync(d_lists, h_lists.data(), h_lists.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st);
-        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
-        if (ce != cudaSuccess) return cuda_error(ce, "pcrp_solve_ragged: system lists");
+    // a batch seen before: its graph, if the workspace has not moved
+    {
+        size_t total = 0;
+        {
+            std::lock_guard<std::mutex> lk(g_mu);
+            auto it = g_exec.find(key);
+            if (it != g_exec.end() && it->second.exec) total = it->second.total;
+        }
+        if (total) {
+            void* ws = nullptr;
+            pcrp_status rc = get_workspace(o, total, st, &ws);
+            if (rc != PCRP_OK) return rc;
+            bool launched = false;
+            int* d_unconv = reinterpret_cast<int*>(static_cast<char*>(ws) +
+                                                   ((size_t)nsys * sizeof(longlong2) + 255) / 256 * 256);
+            {
+                // (launched under the lock: no other thread replaces the graph meanwhile)
+                std::lock_guard<std::mutex> lk(g_mu);
+                auto it = g_exec.find(key);
+                if (it != g_exec.end() && it->second.exec && it->second.ws == ws) {
+                    it->second.used = ++g_clock;
+                    ce = cudaGraphLaunch(it->second.exec, st);
+                    if (ce != cudaSuccess) return cuda_error(ce, "cudaGraphLaunch");
+                    count_launch(it->second.kernels);
+                    launched = true;
+                }
+            }
+            if (launched) {
+                int unconv = 0;
+                ce = cudaMemcpyAsync(&unconv, d_unconv, sizeof(int), cudaMemcpyDeviceToHost, st);
+                if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+                if (ce != cudaSuccess) return cuda_error(ce, "pcrp_solve_ragged");
+                if (unconv)
+                    return set_error(PCRP_ENOCONV, "pcrp_solve_ragged: %d systems did not reach tol=%g in %d sweeps",
+                                     unconv, tol, max_sweeps);
+                return PCRP_OK;
+            }
+        }
     }
 
+    // size classes
+    std::map<int64_t, std::vector<int64_t>> cls;
+    for (int64_t k = 0; k < nsys; k++) {
+        const int64_t n = off[k + 1] - off[k];
+        if (n > 0) cls[size_class(n)].push_back(k);
+    }
+    if (cls.empty()) return PCRP_OK;                 // only empty systems
+    // workspace: [row tables | counter | per class: mixed scratch]
+    // (every class has its own, so that the classes run concurrently)
+    auto r256 = [](size_t v) { return (v + 255) / 256 * 256; };
+    std::vector<size_t> mix_off;
+    size_t per_class = 0;
+    for (auto& kv : cls) {
+        const int64_t ms = (int64_t)kv.second.size(), N = kv.first;
+        mix_off.push_back(per_class);
+        per_class += r256(mixed_workspace_bytes(ms, N, o, max_sweeps, false, PCRP_LAYOUT_CONTIGUOUS));
+    }
+    const size_t lists = r256((size_t)nsys * sizeof(longlong2));
+    const size_t total = lists + 256 + per_class;
+    void* ws = nullptr;
+    pcrp_status rc = get_workspace(o, total, st, &ws);
+    if (rc != PCRP_OK) return rc;
+    char* base = static_cast<char*>(ws);
+    longlong2* d_rows = reinterpret_cast<longlong2*>(base);
+    int* d_unconv = reinterpret_cast<int*>(base + lists);
+    char* d_class = base + lists + 256;
+
+    // system indices, class after class (the graph turns them into the row table)
+    std::vector<int64_t> h_sys;
+    h_sys.reserve(nsys);
+    for (auto& kv : cls) h_sys.insert(h_sys.end(), kv.second.begin(), kv.second.end());
+    const int64_t cnt = (int64_t)h_sys.size();
+    int64_t* d_sys = nullptr;
+    ce = cudaMalloc(&d_sys, cnt * sizeof(int64_t));
+    if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(d_sys, h_sys.data(), cnt * sizeof(int64_t), cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) {
+        if (d_sys) cudaFree(d_sys);
+        return cuda_error(ce, "pcrp_solve_ragged: system lists");
+    }
+
+    // One graph: the counter reset and the row table, then every size class
+    // on its own branch (mixed solve with its device-side sweep loop, count
+    // of the systems left unconverged), joined at the end.
     cudaGraphExec_t exec = nullptr;
     int64_t kernels = 0;
     {
-        std::lock_guard<std::mutex> lk(g_mu);
-        auto it = g_exec.find(key);
-        if (it != g_exec.end()) { exec = it->second.first; kernels = it->second.second; }
-    }
-    if (!exec) {
-        // One graph: the counter reset, then every size class on its own
-        // branch (gather, mixed solve with its device-side sweep loop,
-        // scatter), joined at the end.
         const size_t ncls = cls.size();
         cudaStream_t cst = nullptr;
         std::vector<cudaStream_t> bst(ncls, nullptr);
@@ -191,30 +238,31 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
         if (ce == cudaSuccess) ce = cudaStreamBeginCapture(cst, cudaStreamCaptureModeRelaxed);
         if (ce == cudaSuccess) {
             cudaError_t le = cudaMemsetAsync(d_unconv, 0, sizeof(int), cst);
+            if (le == cudaSuccess) {
+                rgm_rows_kernel<<<grid_for(cnt), 256, 0, cst>>>(offsets, d_sys, cnt, d_rows);
+                count_launch();
+                le = cudaGetLastError();
+            }
             if (le == cudaSuccess) le = cudaEventRecord(bev[ncls], cst);
             int64_t at = 0;
             size_t q = 0;
             for (auto& kv : cls) {
                 if (le != cudaSuccess || prc != PCRP_OK) break;
                 const int64_t ms = (int64_t)kv.second.size(), N = kv.first;
-                const int64_t* sys = d_lists + at;
+                const longlong2* rows = d_rows + at;
                 at += ms;
-                cudaStream_t cs = bst[q];
-                double* d_pad = reinterpret_cast<double*>(d_class + pad_off[q]);
+                cudaStream_t bs = bst[q];
                 void* d_mix = d_class + mix_off[q];
-                le = cudaStreamWaitEvent(cs, bev[ncls], 0);
+                le = cudaStreamWaitEvent(bs, bev[ncls], 0);
                 if (le != cudaSuccess) break;
-                rgm_gather_kernel<<<grid_for(ms * N), 256, 0, cs>>>(a, b, c, d, e, y, offsets, sys, ms, N, d_pad);
-                count_launch();
-                const int64_t T = ms * N;
                 MpArgs A{};
-                prc = mixed_enqueue(d_pad, d_pad + T, d_pad + 2 * T, d_pad + 3 * T, d_pad + 4 * T, d_pad + 5 * T,
-                                    ms, N, N, 1, tol, max_sweeps, o, false, d_mix, cs, &A);
+                prc = mixed_enqueue(a, b, c, d, e, y, ms, N, N, 1, tol, max_sweeps, o, false, d_mix, bs, &A,
+                                    nullptr, nullptr, rows);
                 if (prc != PCRP_OK) break;
-                rgm_scatter_kernel<<<grid_for(T), 256, 0, cs>>>(d_pad + 5 * T, offsets, sys, ms, N, y, A.status, d_unconv);
+                rgm_count_kernel<<<grid_for(ms), 256, 0, bs>>>(A.status, ms, d_unconv);
                 count_launch();
                 le = cudaGetLastError();
-                if (le == cudaSuccess) le = cudaEventRecord(bev[q], cs);
+                if (le == cudaSuccess) le = cudaEventRecord(bev[q], bs);
                 if (le == cudaSuccess) le = cudaStreamWaitEvent(cst, bev[q], 0);
                 q++;
             }
@@ -228,14 +276,30 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
         for (auto ev : bev) if (ev) cudaEventDestroy(ev);
         for (auto bs : bst) if (bs) cudaStreamDestroy(bs);
         if (cst) cudaStreamDestroy(cst);
-        if (prc != PCRP_OK) return prc;
-        if (ce != cudaSuccess) return cuda_error(ce, "ragged mixed graph capture");
+        if (prc != PCRP_OK || ce != cudaSuccess) {
+            if (exec) cudaGraphExecDestroy(exec);
+            cudaFree(d_sys);
+            if (prc != PCRP_OK) return prc;
+            return cuda_error(ce, "ragged mixed graph capture");
+        }
         std::lock_guard<std::mutex> lk(g_mu);
-        g_exec[key] = {exec, kernels};
+        if (g_exec.size() >= kMaxEntries && g_exec.find(key) == g_exec.end()) {
+            auto old = g_exec.begin();
+            for (auto jt = g_exec.begin(); jt != g_exec.end(); ++jt)
+                if (jt->second.used < old->second.used) old = jt;
+            if (old->second.exec) cudaGraphExecDestroy(old->second.exec);
+            if (old->second.d_sys) cudaFree(old->second.d_sys);
+            g_exec.erase(old);
+        }
+        Entry& E = g_exec[key];
+        E.used = ++g_clock;
+        if (E.exec) cudaGraphExecDestroy(E.exec);          // captured on a workspace that has moved
+        if (E.d_sys) cudaFree(E.d_sys);
+        E.total = total; E.ws = ws; E.exec = exec; E.kernels = kernels; E.d_sys = d_sys;
+        ce = cudaGraphLaunch(exec, st);
+        if (ce != cudaSuccess) return cuda_error(ce, "cudaGraphLaunch");
+        count_launch(kernels);
     }
-    ce = cudaGraphLaunch(exec, st);
-    if (ce != cudaSuccess) return cuda_error(ce, "cudaGraphLaunch");
-    count_launch(kernels);
     int unconv = 0;
     ce = cudaMemcpyAsync(&unconv, d_unconv, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);

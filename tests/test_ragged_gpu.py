@@ -125,3 +125,43 @@ def test_ragged_mixed_log_uniform(cuda):
     worst = max(O.fwd_err(x1[offs[k]:offs[k + 1]], xg[offs[k]:offs[k + 1]], 1, int(sizes[k]))
                 for k in range(len(sizes)))
     assert worst <= 1e-12
+
+
+def test_ragged_mixed_reads_no_slot_outside_a_system(cuda):
+    """Mixed mode reads each system in place from the caller's arrays: NaN in
+    every band slot that lies outside its system (a_0, a_1, b_0, d_{n-1},
+    e_{n-2}, e_{n-1}) must not reach any solution.  Sizes sit on both sides
+    of the size-class boundaries (quarter octaves)."""
+    sizes = np.array([33, 40, 41, 48, 49, 56, 57, 64, 65, 1025, 1280, 1281, 4097, 5120, 5121, 7000, 8192, 8193, 2, 3],
+                     dtype=np.int64)
+    arrs, offs = ragged_batch(sizes, 12, garbage=False)
+    for k, n in enumerate(sizes):
+        o = offs[k]
+        arrs[0][o:o + min(2, n)] = np.nan
+        arrs[1][o] = np.nan
+        arrs[3][o + n - 1] = np.nan
+        arrs[4][o + max(n - 2, 0):o + n] = np.nan
+    x = run_ragged(arrs, offs, 1)
+    assert np.isfinite(x).all()
+    clean = [np.nan_to_num(v, nan=0.0) for v in arrs]
+    xg = O.ragged(*clean, offs[:-1], sizes, kind="ge")
+    for k in range(len(sizes)):
+        sl = slice(offs[k], offs[k + 1])
+        assert O.fwd_err(x[sl], xg[sl], 1, int(sizes[k])) <= 1e-12, (k, sizes[k])
+
+
+def test_ragged_mixed_replay_after_workspace_growth(cuda):
+    """The cached graph of a ragged batch is tied to the workspace it was
+    captured on: a larger solve in between (which grows the shared workspace)
+    must lead to a fresh capture, with the same answer."""
+    import torch
+    sizes = np.array([300, 5000, 40, 70000, 1200], dtype=np.int64)
+    arrs, offs = ragged_batch(sizes, 21)
+    x1 = run_ragged(arrs, offs, 1)
+    x2 = run_ragged(arrs, offs, 1)                    # replay
+    rng = np.random.default_rng(5)
+    big = [torch.from_numpy(v).to(cuda) for v in dd_bands(rng, 64, 1 << 17)]
+    pcrp.solve_mixed(*big, 64, 1 << 17)
+    torch.cuda.synchronize()
+    x3 = run_ragged(arrs, offs, 1)
+    assert np.array_equal(x1, x2) and np.array_equal(x1, x3)
