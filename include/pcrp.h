@@ -215,11 +215,14 @@ pcrp_status pcrp_solve_host(const double* a, const double* b, const double* c,
  * occupies rows offsets[k] .. offsets[k+1]-1 of the six arrays (contiguous);
  * `offsets` is a DEVICE array of nsys+1 int64 values with offsets[0] = 0.
  * `a` and `e` may be NULL (zero bands, not read).
- * A device-side work queue bins the systems: those of at most
+ * mode 0 = FP64 PCR-Penta (bit-identical to pcrp_solve_f64 on each system):
+ * a device-side work queue bins the systems; those of at most
  * opts->smem_rows rows are solved whole in shared memory, larger ones are
- * split by global-memory stride passes first.  mode 0 = FP64 PCR-Penta
- * (bit-identical to pcrp_solve_f64 on each system), mode 1 = mixed precision
- * (tol, max_sweeps as in pcrp_solve_mixed).  Queue waits are bounded; a wait
+ * split by global-memory stride passes first.  mode 1 = mixed precision
+ * (tol, max_sweeps as in pcrp_solve_mixed): systems are grouped into size
+ * classes a quarter octave apart, each solved in place as a uniform batch
+ * padded (in the workspace only) with identity rows; PCRP_ENOCONV if a
+ * system misses tol.  Queue waits are bounded; a wait
  * that gives up makes the call return PCRP_ETIMEOUT (reported only when the
  * call synchronises, i.e. always for this entry point).  The launch sequence
  * has a fixed shape for a given (nsys, max rows) and is replayed from a cached

@@ -133,6 +133,8 @@ static int split_strides(int64_t n, int smem_rows)
 }
 
 size_t mixed_workspace_bytes(int64_t m, int64_t n, const pcrp_opts* o, int max_sweeps, bool info, int32_t layout);
+size_t ragged_workspace_bytes(int64_t nsys, int64_t total_rows);
+size_t ragged_mixed_workspace_bound(int64_t nsys, int64_t max_rows, const pcrp_opts* o);
 
 // Whether a solve of n-row systems with these options runs global passes
 // (and so needs split-path scratch); n <= the shared-memory tile needs none.
@@ -294,6 +296,10 @@ pcrp_status pcrp_workspace_size(int64_t m, int64_t n, int32_t layout, int32_t wh
     switch (which) {
     case 0: *bytes = f64_workspace_bytes(m, n, layout, pl, true); return PCRP_OK;
     case 1: *bytes = mixed_workspace_bytes(m, n, opts, 64, true, layout); return PCRP_OK;
+    case 2:                                      // either mode of pcrp_solve_ragged: m systems of <= n rows
+        if (n > 0 && m > (int64_t(1) << 52) / n) return set_error(PCRP_EINVAL, "pcrp_workspace_size: m*n too large");
+        *bytes = std::max(ragged_workspace_bytes(m, m * n), ragged_mixed_workspace_bound(m, n, opts));
+        return PCRP_OK;
     default: return set_error(PCRP_EINVAL, "pcrp_workspace_size: unknown entry family %d", which);
     }
 }

@@ -102,6 +102,20 @@ constexpr size_t kMaxEntries = 16;               // batches remembered (least re
 
 }  // namespace
 
+// An upper bound of the workspace of a mixed ragged batch of nsys systems
+// of at most max_rows rows: every system padded to the largest class, the
+// row table, and the 256-byte rounding of every array of every class (at
+// most four classes per octave of sizes).
+size_t ragged_mixed_workspace_bound(int64_t nsys, int64_t max_rows, const pcrp_opts* o)
+{
+    if (nsys <= 0 || max_rows <= 0) return 0;
+    const int64_t N = size_class(max_rows);
+    const size_t lists = ((size_t)nsys * sizeof(longlong2) + 255) / 256 * 256;
+    const size_t classes = 4 * 64 + 2, arrays = 32;
+    return lists + 256 + mixed_workspace_bytes(nsys, N, o, 64, false, PCRP_LAYOUT_CONTIGUOUS) +
+           classes * arrays * 256;
+}
+
 pcrp_status ragged_mixed(const double* a, const double* b, const double* c, const double* d, const double* e,
                          double* y, const int64_t* offsets, int64_t nsys, int64_t max_rows, double tol,
                          int32_t max_sweeps, const pcrp_opts* o, cudaStream_t st)

@@ -147,3 +147,18 @@ def test_noalloc_accepts_any_batch_of_short_systems_on_cpu(built_lib):
     L = pcrp.lib()
     rc = L.pcrp_solve_f64_noalloc(8, 8, 8, 8, 8, 8, 1 << 20, 512, 0, None)
     assert rc == 2, pcrp.last_error()
+
+
+def test_workspace_size_ragged_family(built_lib):
+    """which=2 (pcrp_solve_ragged) answers a bound for either mode: at least
+    the FP64 mode's state for m*n rows; larger batches need more; an unknown
+    family and an m*n that would wrap are refused."""
+    import pcrp
+    small = pcrp.workspace_size(16, 4096, which=2)
+    big = pcrp.workspace_size(64, 4096, which=2)
+    assert small >= 2 * 7 * 16 * 4096 * 8 and big > small
+    for which in (3, -1):
+        with pytest.raises(pcrp.PcrpError):
+            pcrp.workspace_size(4, 4096, which=which)
+    with pytest.raises(pcrp.PcrpError):
+        pcrp.workspace_size(1 << 40, 1 << 20, which=2)

@@ -165,3 +165,22 @@ def test_ragged_mixed_replay_after_workspace_growth(cuda):
     torch.cuda.synchronize()
     x3 = run_ragged(arrs, offs, 1)
     assert np.array_equal(x1, x2) and np.array_equal(x1, x3)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_ragged_runs_in_the_workspace_it_asks_for(cuda, mode):
+    """A caller-owned workspace of pcrp_workspace_size(nsys, max_rows,
+    which=2) bytes is enough for either mode."""
+    import torch
+    sizes = np.array([33, 1000, 5121, 65536, 7, 40000], dtype=np.int64)
+    arrs, offs = ragged_batch(sizes, 31)
+    need = pcrp.workspace_size(len(sizes), int(sizes.max()), which=2)
+    ws = torch.empty(need, dtype=torch.uint8, device=cuda)
+    x = run_ragged(arrs, offs, mode, pcrp.Opts(workspace=ws.data_ptr(), workspace_bytes=need))
+    if mode == 0:
+        assert_bitexact(x, O.ragged(*arrs, offs[:-1], sizes, kind="pcr"), "caller workspace")
+    else:
+        xg = O.ragged(*arrs, offs[:-1], sizes, kind="ge")
+        for k in range(len(sizes)):
+            sl = slice(offs[k], offs[k + 1])
+            assert O.fwd_err(x[sl], xg[sl], 1, int(sizes[k])) <= 1e-12
