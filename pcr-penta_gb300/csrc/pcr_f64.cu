@@ -87,19 +87,11 @@ cudaError_t launch_rz(const PcrPassArgs& p, int threads, size_t smem, int64_t bl
     return cudaGetLastError();
 }
 
-// Passes whose longest stride reaches kZeroStride rows vote on the zero
-// state: the outer coefficients of diagonally dominant systems underflow at
-// strides ~2^8-2^10, and the vote (~10% of a dense stride) pays once two or
-// more strides of the pass run in that state.  Others keep the plain kernel,
-// unless the batch is tridiagonal (a = e = 0 on entry): then every stride of
-// every pass is in that state and every pass votes.
-constexpr int64_t kZeroStride = 1024;
-
 template <int RPT>
 cudaError_t launch_rpt(const PcrPassArgs& p, bool tridiagonal, int threads, size_t smem, int64_t blocks,
                        cudaStream_t s)
 {
-    if (tridiagonal || (p.K > 0 && (p.G << (p.K - 1)) >= kZeroStride))
+    if (pass_votes(p, tridiagonal))
         return launch_rz<RPT, true>(p, threads, smem, blocks, s);
     return launch_rz<RPT, false>(p, threads, smem, blocks, s);
 }

@@ -67,6 +67,19 @@ struct PcrPassArgs {
                                  // arrays: the tile is staged by bulk asynchronous copies (one per array)
 };
 
+// Passes whose longest stride reaches kZeroStride rows vote on the zero
+// state: the outer coefficients of diagonally dominant systems underflow at
+// strides ~2^8-2^10, and the vote (~10% of a dense stride) pays once two or
+// more strides of the pass run in that state.  Others run without it, unless
+// the batch is tridiagonal (a = e = 0 on entry): then every stride of every
+// pass is in that state and every pass votes.  (Same bits either way.)
+constexpr int64_t kZeroStride = 1024;
+__host__ __device__ inline bool pass_votes(const PcrPassArgs& p, bool tridiagonal)
+{
+    return tridiagonal || (p.K > 0 && (p.G << (p.K - 1)) >= kZeroStride);
+}
+
+
 // Host-side launchers (pcr_f64.cu).  `tridiagonal`: the batch entered with
 // a = e = 0, so every pass compiles in the zero-state vote.
 cudaError_t launch_pcr_pass(const PcrPassArgs& p, int threads, cudaStream_t s, bool tridiagonal = false);
