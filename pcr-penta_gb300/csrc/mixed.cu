@@ -211,25 +211,6 @@ __device__ __forceinline__ PairRow load_pair(const MpArgs& p, int64_t j, int64_t
     return P;
 }
 
-// Rows i0, i0+1 of the rhs of system j -> the contiguous copy Yc (zero on a
-// ragged system's padding rows).
-template <bool RG>
-__device__ __forceinline__ void copy_rhs_pair(const MpArgs& p, int64_t j, int64_t i0)
-{
-    const int64_t n = p.n;
-    double y0, y1 = 0.0;
-    if (RG) {
-        const longlong2 g = __ldg(p.rg + j);
-        y0 = i0 < g.y ? p.y[g.x + i0] : 0.0;
-        if (i0 + 1 < g.y) y1 = p.y[g.x + i0 + 1];
-    } else {
-        y0 = p.y[j * p.ss + i0 * p.rs];
-        if (i0 + 1 < n) y1 = p.y[j * p.ss + (i0 + 1) * p.rs];
-    }
-    p.Yc[j * n + i0] = y0;
-    if (i0 + 1 < n) p.Yc[j * n + i0 + 1] = y1;
-}
-
 // The FP32 row-scaled diagonal block and couplings of block row k (rows
 // i0 = 2k, i1 = 2k+1) of a system with n rows.  Row i1 = n (odd n) is a
 // dummy identity row.  Out-of-range band slots are never read as values.
@@ -266,7 +247,7 @@ __device__ __forceinline__ BlockRow block_of(const PairRow& P, int64_t i0, int64
 // ---------------------------------------------------------------------------
 // One block row of the prep work: row scaling, FP32 blocks, diagonal inverse,
 // the normalised couplings and rhs.
-struct PrepRow { M2 L, U, Mi; float2 Y; };
+struct PrepRow { M2 L, U, Mi; float2 Y; double2 y; };   // y: the two FP64 rhs values (0 past the system)
 
 template <bool RG>
 __device__ __forceinline__ PrepRow prep_row(const MpArgs& p, int64_t j, int64_t k)
@@ -280,7 +261,21 @@ __device__ __forceinline__ PrepRow prep_row(const MpArgs& p, int64_t j, int64_t 
     const float y0 = d2f_scaled(P.y0, B.sh0);
     const float y1 = 2 * k + 1 < p.n ? d2f_scaled(P.y1, B.sh1) : 0.0f;
     r.Y = make_float2(fmaf(r.Mi.m0, y0, r.Mi.m1 * y1), fmaf(r.Mi.m2, y0, r.Mi.m3 * y1));
+    r.y = make_double2(P.y0, 2 * k + 1 < p.n ? P.y1 : 0.0);
     return r;
+}
+
+// Rows i0 = 2k, i0 + 1 of the rhs of system j (loaded by prep_row) -> the
+// contiguous copy Yc, one 16-byte store where the pair is aligned.
+__device__ __forceinline__ void store_rhs_pair(const MpArgs& p, int64_t j, int64_t i0, double2 y)
+{
+    const int64_t q = j * p.n + i0;
+    if (i0 + 1 < p.n) {
+        if ((q & 1) == 0) *reinterpret_cast<double2*>(p.Yc + q) = y;   // (Yc is 256-byte aligned)
+        else { p.Yc[q] = y.x; p.Yc[q + 1] = y.y; }
+    } else {
+        p.Yc[q] = y.x;
+    }
 }
 
 __device__ __forceinline__ void prep_store(const MpArgs& p, int64_t q, const PrepRow& r)
@@ -319,8 +314,9 @@ mp_prep_kernel(MpArgs p)
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = q / nb, k = q - j * nb;
-        prep_store(p, q, prep_row<RG>(p, j, k));
-        copy_rhs_pair<RG>(p, j, 2 * k);
+        const PrepRow r = prep_row<RG>(p, j, k);
+        prep_store(p, q, r);
+        store_rhs_pair(p, j, 2 * k, r.y);
     }
     pdl_release();                                // (multi-wave grid: release once this CTA is done)
 }
@@ -618,7 +614,7 @@ __device__ __forceinline__ void first_item(const MpArgs& p, const MpWindows& g, 
         sL[sk] = f4(r.L); sU[sk] = f4(r.U); sY[sk] = r.Y;
         if (kb >= wlo && kb < whi) {
             prep_store(p, j * nb + kb, r);
-            copy_rhs_pair<RG>(p, j, 2 * kb);
+            store_rhs_pair(p, j, 2 * kb, r.y);
         }
     }
     __syncthreads();
