@@ -38,6 +38,7 @@
 #include "pcrp_internal.h"
 #include "mixed_internal.h"
 #include "mixed_dev.cuh"
+#include "tma.cuh"
 
 namespace pcrp {
 namespace {
@@ -167,10 +168,27 @@ __device__ __forceinline__ void mp_resolve(MpPassArgs& p)
 // system).
 struct PairRow { double a0, a1, b0, b1, c0, c1, d0, d1, e0, e1, y0, y1; };
 
+// L2 residency of the band loads of sweep 0: the prep loads a tile's bands
+// to keep (the residual of the same tile reads them again once its cyclic
+// reduction is done), the residual loads them for the last time.
+enum class Keep { normal, last, first };
+
+__device__ __forceinline__ double2 ldg2_policy(const double* q, uint64_t pol)
+{
+    double2 v;
+    asm("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(q), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ double2 ldg2(const double* q, Keep keep, uint64_t pol)
+{
+    return keep == Keep::normal ? *reinterpret_cast<const double2*>(q) : ldg2_policy(q, pol);
+}
+
 // RG: the batch is ragged (p.rg non-null); the uniform kernels are compiled
 // without the ragged addressing.
 template <bool RG>
-__device__ __forceinline__ PairRow load_pair(const MpArgs& p, int64_t j, int64_t i0)
+__device__ __forceinline__ PairRow load_pair(const MpArgs& p, int64_t j, int64_t i0, Keep keep = Keep::normal)
 {
     PairRow P;
     int64_t n = p.n, rs = p.rs, base = j * p.ss;
@@ -185,12 +203,14 @@ __device__ __forceinline__ PairRow load_pair(const MpArgs& p, int64_t j, int64_t
     const int64_t g0 = base + i0 * rs;
     const double2 z = make_double2(0.0, 0.0);
     if (p.vec && rs == 1 && ((g0 & 1) == 0) && i0 + 1 < n) {
-        const double2 a = p.a ? *reinterpret_cast<const double2*>(p.a + g0) : z;
-        const double2 b = *reinterpret_cast<const double2*>(p.b + g0);
-        const double2 c = *reinterpret_cast<const double2*>(p.c + g0);
-        const double2 d = *reinterpret_cast<const double2*>(p.d + g0);
-        const double2 e = p.e ? *reinterpret_cast<const double2*>(p.e + g0) : z;
-        const double2 y = *reinterpret_cast<const double2*>(p.y + g0);
+        const uint64_t pol = keep == Keep::last ? tma::policy_evict_last()
+                             : keep == Keep::first ? tma::policy_evict_first() : 0;
+        const double2 a = p.a ? ldg2(p.a + g0, keep, pol) : z;
+        const double2 b = ldg2(p.b + g0, keep, pol);
+        const double2 c = ldg2(p.c + g0, keep, pol);
+        const double2 d = ldg2(p.d + g0, keep, pol);
+        const double2 e = p.e ? ldg2(p.e + g0, keep, pol) : z;
+        const double2 y = ldg2(p.y + g0, keep, pol);
         P = {a.x, a.y, b.x, b.y, c.x, c.y, d.x, d.y, e.x, e.y, y.x, y.y};
     } else {
         P.a0 = p.a ? p.a[g0] : 0.0; P.b0 = p.b[g0]; P.c0 = p.c[g0]; P.d0 = p.d[g0];
@@ -250,9 +270,9 @@ __device__ __forceinline__ BlockRow block_of(const PairRow& P, int64_t i0, int64
 struct PrepRow { M2 L, U, Mi; float2 Y; double2 y; };   // y: the two FP64 rhs values (0 past the system)
 
 template <bool RG>
-__device__ __forceinline__ PrepRow prep_row(const MpArgs& p, int64_t j, int64_t k)
+__device__ __forceinline__ PrepRow prep_row(const MpArgs& p, int64_t j, int64_t k, Keep keep = Keep::normal)
 {
-    const PairRow P = load_pair<RG>(p, j, 2 * k);
+    const PairRow P = load_pair<RG>(p, j, 2 * k, keep);
     const BlockRow B = block_of(P, 2 * k, p.n);
     PrepRow r;
     r.Mi = minv(B.D);
@@ -609,7 +629,7 @@ __device__ __forceinline__ void first_item(const MpArgs& p, const MpWindows& g, 
 
     for (int k = tid; k < TR; k += bd) {
         const int64_t kb = t0 + k;
-        const PrepRow r = prep_row<RG>(p, j, kb);
+        const PrepRow r = prep_row<RG>(p, j, kb, Keep::last);
         const int sk = swz(k);
         sL[sk] = f4(r.L); sU[sk] = f4(r.U); sY[sk] = r.Y;
         if (kb >= wlo && kb < whi) {
@@ -661,7 +681,7 @@ __device__ __forceinline__ void first_item(const MpArgs& p, const MpWindows& g, 
     // refinement kernel), row-scaled and normalised -> the rhs of sweep 1
     for (int k = klo + tid; k < khi; k += bd) {
         const int64_t kb = t0 + k, i0 = 2 * kb;
-        const PairRow P = load_pair<RG>(p, j, i0);
+        const PairRow P = load_pair<RG>(p, j, i0, Keep::first);
         const double2 xm = k > 0 ? sX[swz(k - 1)] : make_double2(0.0, 0.0);
         const double2 xc = sX[swz(k)];
         const double2 xp = k + 1 < TR ? sX[swz(k + 1)] : make_double2(0.0, 0.0);
