@@ -86,8 +86,10 @@ struct Key {
 
 // The batch's graph, the workspace it was captured on, and the device list
 // of system indices (class after class) it reads; everything per call is in
-// the graph, so a replay needs no upload.
+// the graph, so a replay needs no upload.  The offsets it was built for are
+// kept and compared on every hit (the key holds only their hash).
 struct Entry {
+    std::vector<int64_t> off;
     size_t total = 0;                 // workspace bytes
     void* ws = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -157,7 +159,7 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
         {
             std::lock_guard<std::mutex> lk(g_mu);
             auto it = g_exec.find(key);
-            if (it != g_exec.end() && it->second.exec) total = it->second.total;
+            if (it != g_exec.end() && it->second.exec && it->second.off == off) total = it->second.total;
         }
         if (total) {
             void* ws = nullptr;
@@ -170,7 +172,7 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
                 // (launched under the lock: no other thread replaces the graph meanwhile)
                 std::lock_guard<std::mutex> lk(g_mu);
                 auto it = g_exec.find(key);
-                if (it != g_exec.end() && it->second.exec && it->second.ws == ws) {
+                if (it != g_exec.end() && it->second.exec && it->second.ws == ws && it->second.off == off) {
                     it->second.used = ++g_clock;
                     ce = cudaGraphLaunch(it->second.exec, st);
                     if (ce != cudaSuccess) return cuda_error(ce, "cudaGraphLaunch");
@@ -309,6 +311,7 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
         E.used = ++g_clock;
         if (E.exec) cudaGraphExecDestroy(E.exec);          // captured on a workspace that has moved
         if (E.d_sys) cudaFree(E.d_sys);
+        E.off = off;
         E.total = total; E.ws = ws; E.exec = exec; E.kernels = kernels; E.d_sys = d_sys;
         ce = cudaGraphLaunch(exec, st);
         if (ce != cudaSuccess) return cuda_error(ce, "cudaGraphLaunch");
