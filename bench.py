@@ -412,6 +412,44 @@ def run_ours(args, world, rank, local, pg):
                              "reciprocal, so frac is the rate of the reference's operations, not the "
                              "FP64 pipe's busy share (ncu reports that)"}
 
+    # end to end through the public API with host buffers (pinned): pcrp_solve_host
+    # (measured before the comparison legs: a long cuSPARSE run leaves the
+    # GPU slower for a while, which is no property of this path)
+    # copies each step's six input arrays in and the solution out, in chunks
+    # that overlap the solves; y is solved in place (the next step's rhs is the
+    # previous solution, same work)
+    h_in = [torch.empty(m * n, dtype=torch.float64, pin_memory=True) for _ in range(6)]
+    pcrp.generate_into(cfg["kind"], seed, m, n, lay, h_in)
+    e_steps = max(2, min(args.steps, 5))
+    precision = 0 if args.solver == "f64" else 1
+
+    def e2e_step():
+        pcrp.solve_host(*h_in, m, n, lay, precision=precision, stream=stream)
+
+    with torch.cuda.stream(stream):
+        e2e_step()
+    stream.synchronize()
+    barrier()
+    # each step ends with the host holding y (it waits for the copy out), so
+    # the next step's copies do not overlap this step's solve
+    ee0 = torch.cuda.Event(enable_timing=True)
+    ee1 = torch.cuda.Event(enable_timing=True)
+    e_list = []
+    with ClockSampler(local) as e_clk:
+        with torch.cuda.stream(stream):
+            for _ in range(e_steps):
+                ee0.record(stream)
+                e2e_step()
+                ee1.record(stream)
+                ee1.synchronize()
+                e_list.append(ee0.elapsed_time(ee1))
+    e_ms = sum(e_list) / e_steps
+    if pg is not None:
+        t = torch.tensor([e_ms], dtype=torch.float64, device=dev if pg.get_backend() == "nccl" else "cpu")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e_ms = float(t.item())
+    e2e_val = world * m * n / (e_ms * 1e-3) / 1e9
+
     # comparison legs (cuSPARSE, the other layout) time at most 5 solves: one
     # cuSPARSE solve of the m=64 n=2^20 batch takes ~6 s
     cmp_reps = min(max(3, args.steps), 5)
@@ -514,40 +552,6 @@ def run_ours(args, world, rank, local, pg):
                       "same_bits_as_headline": same, "checked": f"first {min(m, 16)} systems"}
         del alt, alt_rhs
 
-    # end to end through the public API with host buffers (pinned): pcrp_solve_host
-    # copies each step's six input arrays in and the solution out, in chunks
-    # that overlap the solves; y is solved in place (the next step's rhs is the
-    # previous solution, same work)
-    h_in = [torch.empty(m * n, dtype=torch.float64, pin_memory=True) for _ in range(6)]
-    pcrp.generate_into(cfg["kind"], seed, m, n, lay, h_in)
-    e_steps = max(2, min(args.steps, 5))
-    precision = 0 if args.solver == "f64" else 1
-
-    def e2e_step():
-        pcrp.solve_host(*h_in, m, n, lay, precision=precision, stream=stream)
-
-    with torch.cuda.stream(stream):
-        e2e_step()
-    stream.synchronize()
-    barrier()
-    # each step ends with the host holding y (it waits for the copy out), so
-    # the next step's copies do not overlap this step's solve
-    ee0 = torch.cuda.Event(enable_timing=True)
-    ee1 = torch.cuda.Event(enable_timing=True)
-    e_list = []
-    with torch.cuda.stream(stream):
-        for _ in range(e_steps):
-            ee0.record(stream)
-            e2e_step()
-            ee1.record(stream)
-            ee1.synchronize()
-            e_list.append(ee0.elapsed_time(ee1))
-    e_ms = sum(e_list) / e_steps
-    if pg is not None:
-        t = torch.tensor([e_ms], dtype=torch.float64, device=dev if pg.get_backend() == "nccl" else "cpu")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e_ms = float(t.item())
-    e2e_val = world * m * n / (e_ms * 1e-3) / 1e9
 
     if rank != 0:
         return
@@ -573,7 +577,8 @@ def run_ours(args, world, rank, local, pg):
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 6 * 8 * m * n,
                 "d2h_bytes_per_step": 8 * m * n, "ms_per_step": e_ms,
                 "timing": f"pcrp_solve_host on pinned host buffers, each of {e_steps} steps timed alone "
-                          "(copies in, solve, copy out; the host waits for y before the next step)"},
+                          "(copies in, solve, copy out; the host waits for y before the next step)",
+                "clocks": e_clk.summary()},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
                      "traffic_note": traffic_note,
