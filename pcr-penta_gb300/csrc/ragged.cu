@@ -137,22 +137,44 @@ rg_persistent_kernel(RgArgs a)
 {
     extern __shared__ double smem[];
     __shared__ long long s_item;
+    __shared__ long long s_slot;
     __shared__ int s_skip;
     const int64_t total_slots = (int64_t)kMaxLevels * a.nsys;
     const int64_t total = a.start[total_slots];
+    // Thread 0 claims the CTA's next item while the current one runs, so the
+    // atomic's round trip is off the critical path.  (No wait can deadlock on
+    // an item claimed but not started: waits go to items of lower levels,
+    // which the queue orders first, and the lowest unfinished item is always
+    // the one its CTA is running.)
+    unsigned long long next = 0;
+    if (threadIdx.x == 0) next = atomicAdd(a.head, 1ull);
     for (;;) {
-        if (threadIdx.x == 0) s_item = (long long)atomicAdd(a.head, 1ull);
+        if (threadIdx.x == 0) { s_item = (long long)next; next = atomicAdd(a.head, 1ull); }
         __syncthreads();
         const int64_t item = s_item;
         if (item >= total) break;
-        // slot = last (level, system) whose start <= item
-        int64_t lo = 0, hi = total_slots - 1;
-        while (lo < hi) {
-            const int64_t mid = (lo + hi + 1) / 2;
-            if (a.start[mid] <= item) lo = mid; else hi = mid - 1;
+        // slot = last (level, system) whose start <= item, by warp 0 in
+        // 32-way steps: each round the lanes probe 32 evenly spaced slots of
+        // [lo, hi] and keep the span after the last probe at or below item
+        // (start never decreases; start[lo] <= item throughout).  (The last
+        // slot whose start <= item is never empty: an empty slot shares its
+        // start with the next slot, and item < total.)
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            int64_t lo = 0, hi = total_slots - 1;
+            while (lo < hi) {
+                const int64_t step = (hi - lo + 32) / 32;           // 32 * step > hi - lo
+                const int64_t probe = min(lo + lane * step, hi);
+                const unsigned ok = __ballot_sync(0xffffffffu, a.start[probe] <= item);   // lane 0: probe lo
+                const int best = 31 - __clz((int)ok);
+                const int64_t nlo = min(lo + best * step, hi);
+                hi = min(nlo + step - 1, hi);
+                lo = nlo;
+            }
+            if (lane == 0) s_slot = lo;
         }
-        // (the last slot whose start <= item is never empty: an empty slot shares
-        //  its start with the next slot, and item < total)
+        __syncthreads();
+        const int64_t lo = s_slot;
         const int lvl = (int)(lo / a.nsys);
         const int64_t k = lo - (int64_t)lvl * a.nsys;
         const int64_t i = item - a.start[lo];
