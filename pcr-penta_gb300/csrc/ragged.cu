@@ -42,6 +42,13 @@ constexpr int kMaxLevels = 24;             // global levels + finish
 constexpr long long kSpinLimit = 1LL << 24;
 constexpr long long kSpinLimitInjected = 1LL << 14;   // ~4 ms: the failure-detection test
 
+// One level of one system's plan (computed once per launch by the plan
+// kernel, read by each item of that level).
+struct RgLevel {
+    int64_t G, nwin;                       // gather stride before the level, windows per subsystem
+    int K, H, Lw, P;                       // strides, halo, tile rows; P: the system's global levels
+};
+
 struct RgArgs {
     const double* src[6];                  // caller bands + rhs
     double* y;                             // solution out
@@ -52,6 +59,7 @@ struct RgArgs {
     int64_t* count;                        // [kMaxLevels][nsys] items per (level, system)
     int64_t* start;                        // [kMaxLevels*nsys + 1] exclusive prefix, level-major
     unsigned* done;                        // [kMaxLevels][nsys] finished items
+    RgLevel* lv;                           // [kMaxLevels][nsys] plan of each (level, system)
     unsigned long long* head;              // next item to claim
     int* err;                              // 1: a wait gave up
     int inject;                            // test hook: system 0 waits for an item that never comes
@@ -94,6 +102,11 @@ __global__ void rg_plan_kernel(RgArgs a)
         int K[kMaxLevels], H[kMaxLevels], Lw[kMaxLevels];
         int64_t G[kMaxLevels], nwin[kMaxLevels];
         int P = n > 0 ? rg_plan(n, a.cap, a.fuse, a.L, K, G, nwin, H, Lw) : -1;
+        for (int l = 0; l <= P; l++) {
+            RgLevel v;
+            v.G = G[l]; v.nwin = nwin[l]; v.K = K[l]; v.H = H[l]; v.Lw = Lw[l]; v.P = P;
+            a.lv[(int64_t)l * a.nsys + k] = v;
+        }
         for (int l = 0; l < kMaxLevels; l++) {
             int64_t c = 0;
             if (l < P) c = G[l] * nwin[l];
@@ -179,9 +192,7 @@ rg_persistent_kernel(RgArgs a)
         const int64_t k = lo - (int64_t)lvl * a.nsys;
         const int64_t i = item - a.start[lo];
         const int64_t n = a.offsets[k + 1] - a.offsets[k];
-        int K[kMaxLevels], H[kMaxLevels], Lw[kMaxLevels];
-        int64_t G[kMaxLevels], nwin[kMaxLevels];
-        const int P = rg_plan(n, a.cap, a.fuse, a.L, K, G, nwin, H, Lw);
+        const RgLevel lv = a.lv[lo];                  // (written by the plan kernel before this launch)
 
         // wait for the previous level of this system
         if (threadIdx.x == 0) {
@@ -202,7 +213,7 @@ rg_persistent_kernel(RgArgs a)
         __syncthreads();
         if (!s_skip) {
             PcrPassArgs p;
-            const bool fin = lvl == P;
+            const bool fin = lvl == lv.P;
             for (int u = 0; u < NSTATE; u++) {
                 p.src[u] = lvl == 0 ? (u < 6 ? a.src[u] : nullptr) : a.buf[(lvl - 1) & 1][u];
                 p.dst[u] = fin ? nullptr : a.buf[lvl & 1][u];
@@ -210,9 +221,9 @@ rg_persistent_kernel(RgArgs a)
             p.x = a.y;
             p.offsets = a.offsets;
             p.src_ss = 0; p.src_rs = 1; p.dst_ss = 0; p.dst_rs = 1;
-            p.n = n; p.m = a.nsys; p.G = G[lvl];
-            p.K = K[lvl]; p.final_step = fin ? 1 : 0; p.L = Lw[lvl]; p.H = H[lvl];
-            p.nwin = nwin[lvl];
+            p.n = n; p.m = a.nsys; p.G = lv.G;
+            p.K = lv.K; p.final_step = fin ? 1 : 0; p.L = lv.Lw; p.H = lv.H;
+            p.nwin = lv.nwin;
             p.TRmax = a.cap;
             // subsystem-major pass state, as in the uniform planner: each
             // level's output groups every subsystem of the next level in one
@@ -222,8 +233,8 @@ rg_persistent_kernel(RgArgs a)
             p.src_sub = lvl > 0 ? 1 : 0;
             p.dst_sub = fin ? 0 : 1;
             p.bulk = 0;                               // (per-thread loads through L2: data of this launch)
-            const int64_t r = fin ? i : i / nwin[lvl];
-            const int64_t w = fin ? 0 : i - r * nwin[lvl];
+            const int64_t r = fin ? i : i / lv.nwin;
+            const int64_t w = fin ? 0 : i - r * lv.nwin;
             pcr_tile<kRgRPT, true>(p, k, r, w, smem);
         }
         __syncthreads();
@@ -268,7 +279,8 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
 size_t ragged_workspace_bytes(int64_t nsys, int64_t total_rows)
 {
     const size_t state = 2 * (size_t)NSTATE * (size_t)total_rows * sizeof(double);
-    const size_t plan = (size_t)kMaxLevels * nsys * (2 * sizeof(int64_t) + sizeof(unsigned)) + 2 * sizeof(int64_t) + 64;
+    const size_t plan = (size_t)kMaxLevels * nsys * (2 * sizeof(int64_t) + sizeof(unsigned) + sizeof(RgLevel)) +
+                        2 * sizeof(int64_t) + 64;
     return (state + 255) / 256 * 256 + plan + 256;
 }
 
@@ -330,6 +342,7 @@ pcrp_status ragged_f64(const double* a, const double* b, const double* c, const 
     A.start = reinterpret_cast<int64_t*>(pp); pp += ((size_t)kMaxLevels * nsys + 1) * sizeof(int64_t);
     A.done = reinterpret_cast<unsigned*>(pp); pp += (size_t)kMaxLevels * nsys * sizeof(unsigned);
     pp = base + ((pp - base) + 15) / 16 * 16;
+    A.lv = reinterpret_cast<RgLevel*>(pp); pp += (size_t)kMaxLevels * nsys * sizeof(RgLevel);
     A.head = reinterpret_cast<unsigned long long*>(pp); pp += 16;
     A.err = reinterpret_cast<int*>(pp);
 
