@@ -263,6 +263,15 @@ int64_t pcrp_kernel_launches(void);
  * reference. */
 pcrp_status pcrp_measure_fp64(double* dfma_per_s, double* ddiv_per_s, pcrp_stream stream);
 
+/* Pipe sharing on this GPU (synchronous, a few milliseconds): one launch of
+ * four CTAs per SM whose even warps run FP64 FMA chains and odd warps FP32
+ * FMA or integer chains, timed with CUDA events in five forms: ms[0] FP64
+ * alone, ms[1] FP32 alone, ms[2] integer alone, ms[3] FP64 + FP32, ms[4]
+ * FP64 + integer.  A pair that shares a pipe takes about the sum of its
+ * parts, one that does not about the longer part.  A diagnostic behind the
+ * design of the mixed-precision kernels; no counterpart in the reference. */
+pcrp_status pcrp_measure_pipes(float* ms, pcrp_stream stream);
+
 /* Checks the FP64 kernels' phase-B quotient (Markstein's correction from the
  * correctly rounded reciprocal, inside its exponent guard) against IEEE
  * division (__ddiv_rn) on `samples` seeded random operand pairs of class

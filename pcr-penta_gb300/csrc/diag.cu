@@ -1,5 +1,7 @@
 // diag.cu -- FP64 throughput probe (pcrp_measure_fp64): the denominator of
-// the FP64-pipe roofline of the bit-faithful path.
+// the FP64-pipe roofline of the bit-faithful path; the FP64 / FP32 / integer
+// pipe-sharing probe (pcrp_measure_pipes); the quotient check of the FP64
+// kernels (pcrp_check_quotients).
 #include <cuda_runtime.h>
 
 #include "pcr_tile.cuh"
@@ -64,6 +66,51 @@ cudaError_t time_ms(Launch launch, cudaStream_t s, float* ms)
     }
     cudaEventDestroy(e0);
     return e;
+}
+
+// Pipe sharing: FP64 FMA chains on the even warps of every CTA, and FP32 FMA
+// or integer (xor-shift-add) chains on the odd warps; which of the three run
+// is selected by `mode` (bit 0 FP64, bit 1 FP32, bit 2 integer).  Timing the
+// parts alone and together shows whether the SM runs them side by side.
+__global__ void __launch_bounds__(kProbeThreads) pipe_probe(double* out, int it64, int it32, int itint, int mode)
+{
+    const int w = threadIdx.x >> 5;
+    if ((mode & 1) && !(w & 1)) {
+        double x[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) x[k] = 1.0 + 1e-3 * (threadIdx.x + k);
+        for (int i = 0; i < it64; i++) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) x[k] = fma(x[k], 0.999999, 1e-6);
+        }
+        if (x[0] + x[1] + x[2] + x[3] == 1234.5) out[0] = x[0];   // keeps the chains alive; never true
+    }
+    if ((mode & 2) && (w & 1)) {
+        float f[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) f[k] = 1.0f + 1e-3f * (threadIdx.x + k);
+        for (int i = 0; i < it32; i++) {
+#pragma unroll
+            for (int k = 0; k < 8; k++) f[k] = fmaf(f[k], 0.999999f, 1e-6f);
+        }
+        float acc = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; k++) acc += f[k];
+        if (acc == 1234.5f) out[0] = acc;
+    }
+    if ((mode & 4) && (w & 1)) {
+        unsigned u[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) u[k] = threadIdx.x * 2654435761u + k;
+        for (int i = 0; i < itint; i++) {
+#pragma unroll
+            for (int k = 0; k < 8; k++) u[k] = (u[k] ^ (u[k] >> 7)) + 0x9E3779B9u;
+        }
+        unsigned acc = 0u;
+#pragma unroll
+        for (int k = 0; k < 8; k++) acc ^= u[k];
+        if (acc == 0x12345678u) out[0] = acc;
+    }
 }
 
 }  // namespace
@@ -179,4 +226,25 @@ extern "C" pcrp_status pcrp_measure_fp64(double* dfma_per_s, double* ddiv_per_s,
     *dfma_per_s = lanes * fma_iters / (ms_fma * 1e-3);
     *ddiv_per_s = lanes * div_iters / (ms_div * 1e-3);
     return PCRP_OK;
+}
+
+extern "C" pcrp_status pcrp_measure_pipes(float* ms, pcrp_stream stream)
+{
+    if (!ms) return set_error(PCRP_EINVAL, "pcrp_measure_pipes: null output");
+    cudaStream_t s = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_error(e, "pcrp_measure_pipes");
+    double* out = nullptr;
+    e = cudaMallocAsync(reinterpret_cast<void**>(&out), sizeof(double), s);
+    if (e != cudaSuccess) return cuda_error(e, "pcrp_measure_pipes allocation");
+    // four CTAs per SM; loop counts that give each part alone about a millisecond on GB300
+    const unsigned grid = (unsigned)sms * 4;
+    const int modes[5] = {1, 2, 4, 3, 5};
+    for (int q = 0; q < 5 && e == cudaSuccess; q++)
+        e = time_ms([&] { pipe_probe<<<grid, kProbeThreads, 0, s>>>(out, 2000, 40000, 10000, modes[q]); count_launch(); },
+                    s, &ms[q]);
+    cudaFreeAsync(out, s);
+    return e == cudaSuccess ? PCRP_OK : cuda_error(e, "pcrp_measure_pipes");
 }

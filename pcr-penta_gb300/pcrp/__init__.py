@@ -84,6 +84,7 @@ _SIGS = {
     "pcrp_version": [],
     "pcrp_kernel_launches": [],
     "pcrp_measure_fp64": [_vp, _vp, _vp],
+    "pcrp_measure_pipes": [_vp, _vp],
     "pcrp_check_quotients": [_i32, ctypes.c_uint64, _i64, _vp, _vp, _vp],
     "pcrp_generate": [_i32, ctypes.c_uint64, _i64, _i64, _i32] + [_vp] * 6 + [_i32],
     "pcrp_generate_device": [_i32, ctypes.c_uint64, _i64, _i64, _i32] + [_vp] * 6 + [_vp],
@@ -252,6 +253,15 @@ def measure_fp64(stream=None):
     f, d = ctypes.c_double(0.0), ctypes.c_double(0.0)
     _check(lib().pcrp_measure_fp64(ctypes.byref(f), ctypes.byref(d), _stream(stream)), "pcrp_measure_fp64")
     return f.value, d.value
+
+
+def measure_pipes(stream=None) -> dict:
+    """Milliseconds of the pipe-sharing probe (pcrp_measure_pipes): FP64,
+    FP32 and integer chains alone, and FP64 beside FP32 or integer work on
+    the other warps of the same SMs; synchronous."""
+    ms = (ctypes.c_float * 5)()
+    _check(lib().pcrp_measure_pipes(ms, _stream(stream)), "pcrp_measure_pipes")
+    return dict(zip(("fp64", "fp32", "int", "fp64+fp32", "fp64+int"), list(ms)))
 
 
 def check_quotients(mode: int, seed: int, samples: int, stream=None):

@@ -403,3 +403,16 @@ def test_mixed_fused_sweeps_mixed_batch_and_nan(cuda, n, monkeypatch):
     assert ei.value.status == 5
     xs = t[5].cpu().numpy()
     assert O.fwd_err(xs[:n], O.ge(*[v[:n] for v in bad], 1, n), 1, n) <= TOL
+
+
+def test_pipe_probe_reports_all_five_timings(cuda):
+    """pcrp_measure_pipes times FP64, FP32 and integer chains alone and
+    FP64 beside each of the others (the measurement behind the mixed
+    kernels' split of work between the pipes): five positive, finite
+    timings, and a pair never faster than its slower part."""
+    import math
+    t = pcrp.measure_pipes()
+    assert set(t) == {"fp64", "fp32", "int", "fp64+fp32", "fp64+int"}
+    assert all(v > 0 and math.isfinite(v) for v in t.values())
+    assert t["fp64+fp32"] >= 0.95 * max(t["fp64"], t["fp32"])
+    assert t["fp64+int"] >= 0.95 * max(t["fp64"], t["int"])
