@@ -184,3 +184,19 @@ def test_ragged_runs_in_the_workspace_it_asks_for(cuda, mode):
         for k in range(len(sizes)):
             sl = slice(offs[k], offs[k + 1])
             assert O.fwd_err(x[sl], xg[sl], 1, int(sizes[k])) <= 1e-12
+
+
+def test_ragged_mixed_reports_unconverged_systems(cuda):
+    """Mixed mode with one refinement sweep and an unreachable tolerance:
+    PCRP_ENOCONV (status 5), never a false success; the same batch then
+    solves to the usual bar with the default settings."""
+    sizes = np.array([40, 3000, 70000, 900, 2], dtype=np.int64)
+    arrs, offs = ragged_batch(sizes, 41)
+    with pytest.raises(pcrp.PcrpError) as ei:
+        run_ragged(arrs, offs, 1, tol=1e-30, max_sweeps=1)
+    assert ei.value.status == 5
+    x = run_ragged(arrs, offs, 1)
+    xg = O.ragged(*arrs, offs[:-1], sizes, kind="ge")
+    for k in range(len(sizes)):
+        sl = slice(offs[k], offs[k + 1])
+        assert O.fwd_err(x[sl], xg[sl], 1, int(sizes[k])) <= 1e-12
