@@ -134,7 +134,7 @@ pcrp_status pcrp_solve_f64_split(const double* a, const double* b, const double*
  * hosts whose GPU memory is fixed at start-up).  Its scratch is a 64 MiB
  * array compiled into the library, which every GPU that loads the library
  * keeps until the process exits.  Systems that fit the shared-memory tile
- * (n <= 960 with the tuned plan) need no scratch and any batch of them is
+ * (n <= 512 with the tuned plan) need no scratch and any batch of them is
  * accepted; longer systems need 128 bytes of scratch per unknown, so a call
  * of those accepts at most m*n <= 524288 unknowns and returns PCRP_EINVAL,
  * with the limit in the error text, for more.  It calls no allocator.  The first call on a device looks up

@@ -29,7 +29,7 @@ namespace pcrp {
 
 // Scratch of the split path: two ping-pong copies of the 8-array pass state
 // (128 bytes per unknown), so this size limits one call of systems longer
-// than the shared-memory tile (n > 960 with the tuned plan) to
+// than the shared-memory tile (n > 512 with the tuned plan) to
 // m*n <= 524288.  Shorter systems are solved whole in shared memory, need
 // no scratch, and have no limit.
 constexpr size_t kPcrpNoallocScratchBytes = size_t(64) << 20;   // 64 MiB

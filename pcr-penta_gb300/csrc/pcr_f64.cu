@@ -61,8 +61,11 @@
 namespace pcrp {
 namespace {
 
+// Three CTAs per SM where shared memory allows (tiles up to ~620 rows): the
+// tile state fits 80 registers without spills up to 4 rows per thread, and
+// the extra warps hide more of the FP64 latency; two for 8 rows per thread.
 template <int RPT, bool kZero>
-__global__ void __launch_bounds__(kMaxThreads, 2)
+__global__ void __launch_bounds__(kMaxThreads, RPT >= 8 ? 2 : 3)
 pcr_pass_kernel(const PcrPassArgs p)
 {
     extern __shared__ double smem[];

@@ -9,11 +9,11 @@
 #define PCRP_TUNED_MP_FUSE 5            // mixed: FP32 block strides fused per global pass
 // FP64 path by system size: {n_max, smem_rows, fuse_strides, tile_rows, threads}
 #define PCRP_TUNED_F64_TABLE { \
-    {512, 1920, 2, 1908, 256}, \
-    {1024, 480, 4, 420, 128}, \
-    {8192, 960, 3, 932, 256}, \
-    {131072, 480, 2, 468, 128}, \
-    {2097152, 960, 3, 932, 256} }
+    {512, 512, 3, 484, 256}, \
+    {1024, 512, 3, 484, 256}, \
+    {8192, 512, 2, 500, 256}, \
+    {131072, 512, 1, 508, 256}, \
+    {2097152, 512, 2, 500, 256} }
 // mixed path by system size: {n_max, block rows in shared memory, fuse_strides}
 #define PCRP_TUNED_MP_TABLE { \
     {1024, 1024, 2}, \

@@ -2,8 +2,9 @@
 
 Times every candidate configuration of the faithful FP64 path and of the
 mixed-precision path on representative batch shapes (CUDA events, median of
-several solves on a resident batch), keeps the fastest per size class, and
-writes
+several solves on a resident batch), keeps the fastest per size class, times
+the plan of the ragged FP64 path (one persistent kernel for every system, so
+one plan for all sizes) on a log-uniform ragged batch, and writes
 
   * a JSON record of every measurement (``--json``), and
   * ``csrc/tuned_params.h`` (``--write``), whose tables the library compiles
@@ -23,15 +24,18 @@ import os
 import statistics
 import time
 
-from . import GEN_DOMINANT, Opts, generate_device, solve_f64, solve_mixed
+from . import GEN_DOMINANT, Opts, generate_device, generate_ragged, ragged_sizes, solve_f64, solve_mixed, \
+    solve_ragged
 from .build import CSRC
 
 # (size-class upper bound n_max, batch m used to time it)
 F64_CLASSES = [(512, 1024), (1024, 1024), (8192, 256), (131072, 64), (1 << 21, 8)]
 MP_CLASSES = [(1024, 2048), (8192, 1024), (131072, 128), (1 << 21, 16)]
+# ragged batch timed for the ragged path's plan: systems, sizes log-uniform in [lo, hi]
+RAGGED_BATCH = (512, 32, 65536)
 
 
-def _timeit(fn, reps=3, warm=1):
+def _timeit(fn, reps=5, warm=1):
     import torch
     s = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -55,11 +59,18 @@ def _batch(m, n, seed=1):
 
 
 def f64_candidates():
-    for smem, fuse, threads in itertools.product((480, 960, 1920), (1, 2, 3, 4, 5), (128, 256)):
+    for smem, fuse, threads in itertools.product((480, 512, 640, 960, 1920), (1, 2, 3, 4, 5), (128, 256)):
         H = 2 * ((1 << fuse) - 1)
         if smem - 2 * H < 64:
             continue
         yield dict(smem_rows=smem, fuse_strides=fuse, tile_rows=smem - 2 * H, threads=threads)
+
+
+def rg_candidates():
+    # the persistent kernel runs 256 threads and up to 1024 rows per tile
+    for smem, fuse in itertools.product((640, 768, 896, 960, 1024), (2, 3, 4)):
+        H = 2 * ((1 << fuse) - 1)
+        yield dict(smem_rows=smem, fuse_strides=fuse, tile_rows=smem - 2 * H, threads=256)
 
 
 def mp_candidates():
@@ -69,14 +80,43 @@ def mp_candidates():
         yield dict(smem_rows=2 * cap, fuse_strides=fuse)
 
 
+def tune_ragged(verbose: bool = True):
+    """Times the ragged path's plan candidates; returns (measurements, best)."""
+    import numpy as np
+    import torch
+    nsys, lo, hi = RAGGED_BATCH
+    sizes = ragged_sizes(1, nsys, lo, hi)
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    arrs = [torch.from_numpy(v).cuda() for v in generate_ragged(GEN_DOMINANT, 1, offs)]
+    rhs = arrs[5].clone()
+    d_off = torch.from_numpy(offs).cuda()
+    meas, best = [], None
+    for c in rg_candidates():
+        o = Opts(**c)
+
+        def run():
+            arrs[5].copy_(rhs)
+            solve_ragged(*arrs, d_off, nsys, int(sizes.max()), mode=0, opts=o)
+        ms = _timeit(run)
+        meas.append(dict(n=int(offs[-1]), m=nsys, opts=c, ms=ms, gunk_s=int(offs[-1]) / ms / 1e6))
+        if best is None or ms < best["ms"]:
+            best = dict(n=int(offs[-1]), m=nsys, ms=ms, opts=c)
+        if verbose:
+            print(f"ragged rows={int(offs[-1])} systems={nsys} {c} {ms:.3f} ms", flush=True)
+    return meas, [best]
+
+
 def tune(budget_s: float = 600.0, verbose: bool = True, only=None):
-    """Times the candidates of both paths (or of `only`: "f64" or "mixed")."""
+    """Times the candidates of both paths and the ragged plan (or only one:
+    "f64", "mixed" or "ragged")."""
     import torch
     t_start = time.time()
     rec = {"device": torch.cuda.get_device_name(0), "f64": [], "mixed": []}
+    if only in (None, "ragged"):
+        rec["ragged"], rec["ragged_best"] = tune_ragged(verbose)
     for kind, classes, cands, solver in (("f64", F64_CLASSES, list(f64_candidates()), solve_f64),
                                          ("mixed", MP_CLASSES, list(mp_candidates()), solve_mixed)):
-        if only and kind != only:
+        if only is not None and kind != only:
             continue
         for n_max, m in classes:
             n = n_max if n_max <= 131072 else n_max // 2
@@ -113,6 +153,7 @@ def tune(budget_s: float = 600.0, verbose: bool = True, only=None):
 def header_text(rec) -> str:
     f64 = rec["f64_best"]
     mp = rec["mixed_best"]
+    rg = rec["ragged_best"][0]["opts"] if rec.get("ragged_best") else f64[-1]["opts"]
     rows_f = ", \\\n    ".join("{%d, %d, %d, %d, %d}" % (b["n_max"], b["opts"]["smem_rows"], b["opts"]["fuse_strides"],
                                                      b["opts"]["tile_rows"], b["opts"]["threads"]) for b in f64)
     rows_m = ", \\\n    ".join("{%d, %d, %d}" % (b["n_max"], b["opts"]["smem_rows"] // 2, b["opts"]["fuse_strides"])
@@ -120,10 +161,10 @@ def header_text(rec) -> str:
     return f"""// tuned_params.h -- defaults chosen by the autotuner (pcrp/autotune.py) on {rec['device']}.
 // Regenerated by `python -m pcrp.autotune --write`; edit there, not here.
 #pragma once
-#define PCRP_TUNED_SMEM_ROWS {f64[-1]['opts']['smem_rows']}     // ragged path: shared-memory capacity (rows)
-#define PCRP_TUNED_FUSE_STRIDES {f64[-1]['opts']['fuse_strides']}     // ragged path: strides fused per global pass
-#define PCRP_TUNED_TILE_ROWS {f64[-1]['opts']['tile_rows']}      // ragged path: rows written per CTA in a global pass
-#define PCRP_TUNED_THREADS {f64[-1]['opts']['threads']}        // threads per CTA
+#define PCRP_TUNED_SMEM_ROWS {rg['smem_rows']}     // ragged path: shared-memory capacity (rows)
+#define PCRP_TUNED_FUSE_STRIDES {rg['fuse_strides']}     // ragged path: strides fused per global pass
+#define PCRP_TUNED_TILE_ROWS {rg['tile_rows']}      // ragged path: rows written per CTA in a global pass
+#define PCRP_TUNED_THREADS {rg['threads']}        // threads per CTA
 #define PCRP_TUNED_MP_SMEM_BLOCKS {mp[-1]['opts']['smem_rows'] // 2}   // mixed: block rows solved whole in shared memory
 #define PCRP_TUNED_MP_FUSE {mp[-1]['opts']['fuse_strides']}            // mixed: FP32 block strides fused per global pass
 // FP64 path by system size: {{n_max, smem_rows, fuse_strides, tile_rows, threads}}
@@ -141,8 +182,8 @@ def main():
     ap.add_argument("--header", default=os.path.join(CSRC, "tuned_params.h"))
     ap.add_argument("--write", action="store_true")
     ap.add_argument("--budget", type=float, default=600.0)
-    ap.add_argument("--only", choices=("f64", "mixed"), default=None,
-                    help="tune one path; the other's results come from --prev")
+    ap.add_argument("--only", choices=("f64", "mixed", "ragged"), default=None,
+                    help="tune one part; the others' results come from --prev")
     ap.add_argument("--prev", default=None, help="earlier JSON record (with --only)")
     args = ap.parse_args()
     rec = tune(args.budget, only=args.only)
@@ -151,8 +192,9 @@ def main():
             ap.error("--only needs --prev, the record that holds the other path's results")
         with open(args.prev) as f:
             prev = json.load(f)
-        other = "mixed" if args.only == "f64" else "f64"
-        rec[other], rec[other + "_best"] = prev[other], prev[other + "_best"]
+        for other in ("f64", "mixed", "ragged"):
+            if other != args.only and other + "_best" in prev:
+                rec[other], rec[other + "_best"] = prev[other], prev[other + "_best"]
     if args.json:
         with open(args.json, "w") as f:
             json.dump(rec, f, indent=1)
