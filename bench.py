@@ -49,10 +49,10 @@ BYTES_PER_UNKNOWN = 56          # 5 FP64 bands + FP64 rhs read once, FP64 x writ
 # config's own layout and the autotuned plan.  The capture commands and the
 # raw figures are kept with the ncu summaries in the repository's profiles.
 MEASURED_TRAFFIC = {
-    ("c1", "f64"): (495.4, "ncu capture m=48 n=65536, the 5 pcr_pass_kernel launches of one solve"),
+    ("c1", "f64"): (831.0, "ncu capture m=48 n=65536, the 8 pcr_pass_kernel launches of one solve"),
     ("c1", "mixed"): (117.5, "ncu capture m=48 n=65536, mp_first_kernel + mp_try_kernel of one solve"),
     ("c2", "mixed"): (123.0, "ncu capture m=1024 n=4096, the mp_small_kernel launch of one solve"),
-    ("c4", "f64"): (516.4, "ncu capture m=4 n=2^20, the 5 pcr_pass_kernel launches of one solve"),
+    ("c4", "f64"): (747.7, "ncu capture m=4 n=2^20, the 7 pcr_pass_kernel launches of one solve"),
     ("c4", "mixed"): (139.2, "ncu capture m=4 n=2^20, mp_first_kernel + mp_try_kernel of one solve"),
 }
 
