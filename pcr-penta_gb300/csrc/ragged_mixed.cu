@@ -64,7 +64,8 @@ unsigned grid_for(int64_t total) {
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152 * 16));
 }
 
-// A batch: its pointers, stream, sizes (hashed) and solver settings.
+// A batch: its pointers, stream, sizes (hashed), solver settings and the
+// tuning fields of its options (they shape the captured plan).
 struct Key {
     int dev;
     cudaStream_t s;
@@ -73,6 +74,7 @@ struct Key {
     uint64_t hash;
     double tol;
     int sweeps;
+    int opt[6];
     bool operator<(const Key& o) const {
         if (dev != o.dev) return dev < o.dev;
         if (s != o.s) return s < o.s;
@@ -80,6 +82,7 @@ struct Key {
         if (nsys != o.nsys) return nsys < o.nsys;
         if (hash != o.hash) return hash < o.hash;
         if (tol != o.tol) return tol < o.tol;
+        for (int q = 0; q < 6; q++) if (opt[q] != o.opt[q]) return opt[q] < o.opt[q];
         return sweeps < o.sweeps;
     }
 };
@@ -152,6 +155,10 @@ pcrp_status ragged_mixed(const double* a, const double* b, const double* c, cons
     const void* ptrs[7] = {a, b, c, d, e, y, offsets};
     for (int q = 0; q < 7; q++) key.p[q] = ptrs[q];
     key.nsys = nsys; key.hash = h; key.tol = tol; key.sweeps = max_sweeps;
+    if (o && o->size >= sizeof(pcrp_opts)) {
+        const int v[6] = {o->smem_rows, o->fuse_strides, o->tile_rows, o->threads, o->reserved0, o->window_levels};
+        for (int q = 0; q < 6; q++) key.opt[q] = v[q];
+    }
 
     // a batch seen before: its graph, if the workspace has not moved
     {
