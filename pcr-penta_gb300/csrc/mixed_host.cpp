@@ -211,7 +211,7 @@ struct GraphKey {
     const void* ptr[9];
     int64_t m, n, ss, rs;
     double tol;
-    int max_sweeps, cap, fuse, win, duo;
+    int max_sweeps, cap, fuse, win, duo, inject;
     bool operator<(const GraphKey& o) const { return std::memcmp(this, &o, sizeof(GraphKey)) < 0; }
 };
 
@@ -323,7 +323,7 @@ pcrp_status launch_sweep_graph(const MpArgs& A, const SweepPlan& S, cudaStream_t
     const void* ptrs[9] = {A.a, A.b, A.c, A.d, A.e, A.y, A.S0, A.xout, A.rg};
     for (int i = 0; i < 9; i++) k.ptr[i] = ptrs[i];
     k.m = A.m; k.n = A.n; k.ss = A.ss; k.rs = A.rs; k.tol = A.tol; k.max_sweeps = A.max_sweeps;
-    k.cap = S.pl.cap; k.fuse = S.pl.fuse; k.win = S.pl.win; k.duo = S.duo;
+    k.cap = S.pl.cap; k.fuse = S.pl.fuse; k.win = S.pl.win; k.duo = S.duo; k.inject = A.inject;
     std::lock_guard<std::mutex> lk(g_graph_mu);
     auto it = g_graphs.find(k);
     if (it == g_graphs.end()) {
