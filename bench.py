@@ -586,6 +586,10 @@ def run_ours(args, world, rank, local, pg):
                              f"({kms_med:.3f} ms); peak {peak_kind}"},
         "clocks": clk.summary(),
     }
+    if small and step_ms:
+        # steps timed one at a time (after an L2 flush): their spread beside the mean
+        q = sorted(step_ms)
+        line["step_ms_spread"] = {"min": q[0], "median": statistics.median(q), "max": q[-1]}
     line["accuracy"] = {"resid": resid, "resid_sample": f"all {m} systems, worst system"}
     if fp64_roof is not None:
         line["fp64_roofline"] = fp64_roof
