@@ -36,7 +36,7 @@ pcrp_status get_workspace(const pcrp_opts* o, size_t bytes, cudaStream_t s, void
 namespace {
 
 constexpr int kRgThreads = 256;
-constexpr int kRgRPT = 4;                  // rows per thread: capacity 1024 rows
+constexpr int kRgRPT = 2;                  // rows per thread: capacity 512 rows
 constexpr int kRgCap = kRgThreads * kRgRPT;
 constexpr int kMaxLevels = 24;             // global levels + finish
 constexpr long long kSpinLimit = 1LL << 24;
@@ -145,7 +145,9 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
     return v;
 }
 
-__global__ void __launch_bounds__(kRgThreads, 2)
+// three CTAs per SM: 512-row tiles fit shared memory three times over, and
+// the state of 2 rows per thread fits 80 registers
+__global__ void __launch_bounds__(kRgThreads, 3)
 rg_persistent_kernel(RgArgs a)
 {
     extern __shared__ double smem[];

@@ -1,9 +1,9 @@
 // tuned_params.h -- defaults chosen by the autotuner (pcrp/autotune.py) on NVIDIA GB300.
 // Regenerated by `python -m pcrp.autotune --write`; edit there, not here.
 #pragma once
-#define PCRP_TUNED_SMEM_ROWS 960     // ragged path: shared-memory capacity (rows)
-#define PCRP_TUNED_FUSE_STRIDES 3     // ragged path: strides fused per global pass
-#define PCRP_TUNED_TILE_ROWS 932      // ragged path: rows written per CTA in a global pass
+#define PCRP_TUNED_SMEM_ROWS 512     // ragged path: shared-memory capacity (rows)
+#define PCRP_TUNED_FUSE_STRIDES 2     // ragged path: strides fused per global pass
+#define PCRP_TUNED_TILE_ROWS 500      // ragged path: rows written per CTA in a global pass
 #define PCRP_TUNED_THREADS 256        // threads per CTA
 #define PCRP_TUNED_MP_SMEM_BLOCKS 1024   // mixed: block rows solved whole in shared memory
 #define PCRP_TUNED_MP_FUSE 5            // mixed: FP32 block strides fused per global pass

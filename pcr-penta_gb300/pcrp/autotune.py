@@ -67,8 +67,8 @@ def f64_candidates():
 
 
 def rg_candidates():
-    # the persistent kernel runs 256 threads and up to 1024 rows per tile
-    for smem, fuse in itertools.product((640, 768, 896, 960, 1024), (2, 3, 4)):
+    # the persistent kernel runs 256 threads and up to 512 rows per tile
+    for smem, fuse in itertools.product((384, 448, 480, 512), (1, 2, 3)):
         H = 2 * ((1 << fuse) - 1)
         yield dict(smem_rows=smem, fuse_strides=fuse, tile_rows=smem - 2 * H, threads=256)
 
