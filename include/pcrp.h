@@ -96,8 +96,14 @@ typedef struct pcrp_mixed_info {
  * 2x2 finish otherwise), then x = y/c.  Every product, sum and IEEE quotient
  * is the one the reference forms, in the same order, without FMA contraction,
  * so the result is bit-identical to the reference kernels built with
- * -fmad=false.  Dispatches like the reference host code (main.cu:46-87):
- * n <= 1024 -> pcrp_solve_f64_small, otherwise pcrp_solve_f64_split.
+ * -fmad=false.  Takes the place of the reference host code's dispatch
+ * (main.cu:46-87: n <= 1024 -> pcr_penta, otherwise the splitting kernels),
+ * with the split point from the tuned plan instead of n = 1024: systems of
+ * at most the plan's shared-memory rows (opts->smem_rows; 512 tuned on
+ * GB300) are solved whole in shared memory, longer ones by global passes
+ * and the shared-memory finish -- the same bits either way.
+ * pcrp_solve_f64_small and pcrp_solve_f64_split keep the reference's own
+ * n = 1024 split.
  * `a` and `e` may be NULL: that band is +0.0 and is not read; with both NULL
  * (a tridiagonal batch) every stride runs the kernels' zero-operand form, with
  * the bits of explicit +0.0 bands.  The same holds for the two paths below,
