@@ -180,3 +180,22 @@ def test_autotune_record_best_is_the_fastest_measured():
         for b in rec.get(kind + "_best", []):
             ms = [r["ms"] for r in rec[kind] if r["n"] == b["n"] and r["m"] == b["m"] and "ms" in r]
             assert ms and b["ms"] == min(ms), (kind, b)
+
+
+def test_autotune_header_ragged_defaults():
+    """The ragged path's defaults come from the record's own ragged search
+    when it has one, else from the largest FP64 size class (older records)."""
+    import copy
+    import json
+    sys.path.insert(0, os.path.join(bench.ROOT, "pcr-penta_gb300"))
+    from pcrp import autotune
+    with open(os.path.join(bench.ROOT, "profiles", "autotune_gb300.json")) as f:
+        rec = json.load(f)
+    rg = rec["ragged_best"][0]["opts"]
+    text = autotune.header_text(rec)
+    assert f"#define PCRP_TUNED_SMEM_ROWS {rg['smem_rows']} " in text
+    assert f"#define PCRP_TUNED_FUSE_STRIDES {rg['fuse_strides']} " in text
+    old = copy.deepcopy(rec)
+    old.pop("ragged_best")
+    last = old["f64_best"][-1]["opts"]
+    assert f"#define PCRP_TUNED_TILE_ROWS {last['tile_rows']} " in autotune.header_text(old)
