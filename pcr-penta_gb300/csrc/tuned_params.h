@@ -16,7 +16,7 @@
     {2097152, 512, 2, 500, 256} }
 // mixed path by system size: {n_max, block rows in shared memory, fuse_strides}
 #define PCRP_TUNED_MP_TABLE { \
-    {1024, 1024, 2}, \
-    {8192, 512, 5}, \
-    {131072, 1024, 6}, \
+    {1024, 2048, 2}, \
+    {8192, 1024, 5}, \
+    {131072, 1024, 5}, \
     {2097152, 1024, 5} }

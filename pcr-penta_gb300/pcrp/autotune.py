@@ -1,8 +1,9 @@
 """Autotuner for the tile sizes, fused-stride depth and shared/global split.
 
 Times every candidate configuration of the faithful FP64 path and of the
-mixed-precision path on representative batch shapes (CUDA events, median of
-several solves on a resident batch), keeps the fastest per size class, times
+mixed-precision path's general passes on representative batch shapes (CUDA
+events, median of several solves on a resident batch), keeps the fastest per
+size class, times
 the plan of the ragged FP64 path (one persistent kernel for every system, so
 one plan for all sizes) on a log-uniform ragged batch, and writes
 
@@ -74,10 +75,14 @@ def rg_candidates():
 
 
 def mp_candidates():
+    # The mixed table steers the general block-PCR passes: the path of systems
+    # longer than one tile that the windowed reduction leaves coupled.  Dominant
+    # systems decouple in the windows, so the candidates run with the windows
+    # off (window_levels = -1) to time the passes the table plans.
     for cap, fuse in itertools.product((256, 512, 1024, 2048), (2, 3, 4, 5, 6, 7)):
         if cap - 2 * ((1 << fuse) - 1) < 32:
             continue
-        yield dict(smem_rows=2 * cap, fuse_strides=fuse)
+        yield dict(smem_rows=2 * cap, fuse_strides=fuse, window_levels=-1)
 
 
 def tune_ragged(verbose: bool = True):
@@ -144,6 +149,8 @@ def tune(budget_s: float = 600.0, verbose: bool = True, only=None):
                     best = (ms, c)
                 if verbose:
                     print(f"{kind} n={n} m={m} {c} {ms:.3f} ms", flush=True)
+            if best is None:
+                raise RuntimeError(f"autotune: no {kind} candidate ran for n={n} m={m} (time budget or errors)")
             rec.setdefault(kind + "_best", []).append(dict(n_max=n_max, n=n, m=m, ms=best[0], opts=best[1]))
             del arrs, rhs
             torch.cuda.empty_cache()
