@@ -162,3 +162,48 @@ def test_workspace_size_ragged_family(built_lib):
             pcrp.workspace_size(4, 4096, which=which)
     with pytest.raises(pcrp.PcrpError):
         pcrp.workspace_size(1 << 40, 1 << 20, which=2)
+
+
+def test_mixed_residual_host_ragged_argument_validation(built_lib):
+    """The other entry points refuse bad arguments before any CUDA call (so
+    without a GPU) and treat empty batches as no-ops, as pcrp.h states."""
+    L = pcrp.lib()
+    info = pcrp.MixedInfo()
+    mixed = L.pcrp_solve_mixed
+    assert mixed(None, None, None, None, None, None, 0, 64, 0, 0.0, 0, None, None, ctypes.byref(info)) == 0
+    assert info.converged == 1                                                   # empty batch: converged
+    assert mixed(None, None, None, None, None, None, 4, 0, 0, 0.0, 0, None, None, None) == 0
+    assert mixed(None, None, None, None, None, None, -1, 64, 0, 0.0, 0, None, None, None) == 1
+    assert mixed(None, None, None, None, None, None, 4, 64, 5, 0.0, 0, None, None, None) == 1   # layout
+    assert mixed(None, None, None, None, None, None, 4, 64, 0, 0.0, 0, None, None, None) == 1   # null arrays
+    assert "null array" in pcrp.last_error()
+    assert mixed(1, 1, 1, 1, 1, 1, 1 << 25, 64, 0, 0.0, 0, None, None, None) == 1               # m > 2^24
+    assert "out of range" in pcrp.last_error()
+    assert mixed(1, 1, 1, 1, 1, 1, 4, (1 << 31) + 2, 0, 0.0, 0, None, None, None) == 1          # n > 2^31
+
+    res = L.pcrp_residual_f64
+    assert res(*([None] * 8), 0, 64, 0, None) == 0
+    assert res(*([None] * 8), -3, 64, 0, None) == 1
+    assert res(*([None] * 8), 4, 64, 9, None) == 1
+    assert res(*([None] * 8), 4, 64, 0, None) == 1
+    assert res(1, 1, 1, 1, 1, 1, 7, 7, 4, 64, 0, None) == 1                                     # r aliases x
+    assert "alias" in pcrp.last_error()
+
+    host = L.pcrp_solve_host
+    assert host(*([None] * 6), 0, 64, 0, 0, 0.0, 0, None, None) == 0
+    assert host(*([None] * 6), -1, 64, 0, 0, 0.0, 0, None, None) == 1
+    assert host(*([None] * 6), 4, 64, 3, 0, 0.0, 0, None, None) == 1                            # layout
+    assert host(*([None] * 6), 4, 64, 0, 2, 0.0, 0, None, None) == 1                            # precision
+    assert "precision" in pcrp.last_error()
+    assert host(*([None] * 6), 4, 64, 0, 1, 0.0, 0, None, None) == 1                            # null arrays
+
+    rg = L.pcrp_solve_ragged
+    assert rg(*([None] * 7), 0, 64, 0, 0.0, 0, None, None) == 0
+    assert rg(*([None] * 7), 8, 0, 1, 0.0, 0, None, None) == 0
+    assert rg(*([None] * 7), -1, 64, 0, 0.0, 0, None, None) == 1
+    assert rg(*([None] * 7), 8, -1, 0, 0.0, 0, None, None) == 1
+    assert rg(*([None] * 7), 8, 64, 2, 0.0, 0, None, None) == 1                                 # mode
+    assert "mode" in pcrp.last_error()
+    assert rg(1, 1, 1, 1, 1, 1, None, 8, 64, 0, 0.0, 0, None, None) == 1                        # null offsets
+    assert rg(1, 1, 1, 1, 1, 1, 1, (1 << 24) + 1, 64, 1, 0.0, 0, None, None) == 1               # nsys > 2^24
+    assert "out of range" in pcrp.last_error()
