@@ -248,19 +248,60 @@ rg_persistent_kernel(RgArgs a)
 }
 
 // Cached CUDA graph of the launch sequence, per (device, stream, arguments).
+// The total row count is part of the key: it sets where the workspace's
+// state arrays and queue plan lie, which the captured kernels hold.
 struct GraphKey {
     int dev;
     cudaStream_t s;
     const void* ptrs[8];
-    int64_t nsys, max_rows;
+    int64_t nsys, max_rows, total;
     int cap, fuse, L;
     bool operator<(const GraphKey& o) const {
-        return std::tie(dev, s, ptrs[0], ptrs[1], ptrs[2], ptrs[3], ptrs[4], ptrs[5], ptrs[6], ptrs[7], nsys, max_rows, cap, fuse, L) <
-               std::tie(o.dev, o.s, o.ptrs[0], o.ptrs[1], o.ptrs[2], o.ptrs[3], o.ptrs[4], o.ptrs[5], o.ptrs[6], o.ptrs[7], o.nsys, o.max_rows, o.cap, o.fuse, o.L);
+        return std::tie(dev, s, ptrs[0], ptrs[1], ptrs[2], ptrs[3], ptrs[4], ptrs[5], ptrs[6], ptrs[7], nsys, max_rows,
+                        total, cap, fuse, L) <
+               std::tie(o.dev, o.s, o.ptrs[0], o.ptrs[1], o.ptrs[2], o.ptrs[3], o.ptrs[4], o.ptrs[5], o.ptrs[6],
+                        o.ptrs[7], o.nsys, o.max_rows, o.total, o.cap, o.fuse, o.L);
     }
 };
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    uint64_t used = 0;
+};
 std::mutex g_graph_mu;
-std::map<GraphKey, cudaGraphExec_t> g_graphs;
+std::map<GraphKey, GraphEntry> g_graphs;
+uint64_t g_graph_clock = 0;
+constexpr size_t kMaxGraphs = 16;                 // batches remembered (least recently used dropped)
+
+// Launches the cached graph of `key` on `st` (under the lock, so that no
+// other thread drops it meanwhile); false if there is none.
+bool launch_cached(const GraphKey& key, cudaStream_t st, cudaError_t* ce)
+{
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    auto it = g_graphs.find(key);
+    if (it == g_graphs.end() || !it->second.exec) return false;
+    it->second.used = ++g_graph_clock;
+    *ce = cudaGraphLaunch(it->second.exec, st);
+    return true;
+}
+
+// Remembers `exec` for `key` (replacing an entry another thread made
+// meanwhile, dropping the least recently used one when full) and launches it.
+cudaError_t remember_and_launch(const GraphKey& key, cudaGraphExec_t exec, cudaStream_t st)
+{
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    if (g_graphs.size() >= kMaxGraphs && g_graphs.find(key) == g_graphs.end()) {
+        auto old = g_graphs.begin();
+        for (auto jt = g_graphs.begin(); jt != g_graphs.end(); ++jt)
+            if (jt->second.used < old->second.used) old = jt;
+        if (old->second.exec) cudaGraphExecDestroy(old->second.exec);   // (freed when a launch in flight ends)
+        g_graphs.erase(old);
+    }
+    GraphEntry& E = g_graphs[key];
+    if (E.exec) cudaGraphExecDestroy(E.exec);
+    E.exec = exec;
+    E.used = ++g_graph_clock;
+    return cudaGraphLaunch(exec, st);
+}
 
 cudaError_t enqueue(const RgArgs& a, int grid, cudaStream_t s)
 {
@@ -364,14 +405,10 @@ pcrp_status ragged_f64(const double* a, const double* b, const double* c, const 
     key.dev = dev; key.s = st;
     const void* ptrs[8] = {a, b, c, d, e, y, offsets, ws};
     for (int q = 0; q < 8; q++) key.ptrs[q] = ptrs[q];
-    key.nsys = nsys; key.max_rows = max_rows; key.cap = cap; key.fuse = fuse; key.L = L + (A.inject << 20);
-    cudaGraphExec_t exec = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(g_graph_mu);
-        auto it = g_graphs.find(key);
-        if (it != g_graphs.end()) exec = it->second;
-    }
-    if (!exec) {
+    key.nsys = nsys; key.max_rows = max_rows; key.total = total_rows_bound;
+    key.cap = cap; key.fuse = fuse; key.L = L + (A.inject << 20);
+    if (!launch_cached(key, st, &ce)) {
+        cudaGraphExec_t exec = nullptr;
         cudaStream_t cap_s = nullptr;
         ce = cudaStreamCreateWithFlags(&cap_s, cudaStreamNonBlocking);
         if (ce != cudaSuccess) return cuda_error(ce, "cudaStreamCreate");
@@ -385,11 +422,12 @@ pcrp_status ragged_f64(const double* a, const double* b, const double* c, const 
         if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, g, 0);
         if (g) cudaGraphDestroy(g);
         cudaStreamDestroy(cap_s);
-        if (ce != cudaSuccess) return cuda_error(ce, "ragged graph capture");
-        std::lock_guard<std::mutex> lk(g_graph_mu);
-        g_graphs[key] = exec;
+        if (ce != cudaSuccess) {
+            if (exec) cudaGraphExecDestroy(exec);
+            return cuda_error(ce, "ragged graph capture");
+        }
+        ce = remember_and_launch(key, exec, st);
     }
-    ce = cudaGraphLaunch(exec, st);
     if (ce != cudaSuccess) return cuda_error(ce, "cudaGraphLaunch");
     count_launch(3);                       // the graph's three kernels
     int err = 0;

@@ -168,6 +168,39 @@ def test_ragged_mixed_replay_after_workspace_growth(cuda):
 
 
 @pytest.mark.parametrize("mode", [0, 1])
+def test_ragged_replay_with_offsets_rewritten_in_place(cuda, mode):
+    """The same arrays, offsets buffer and caller workspace, the offsets
+    rewritten between calls to a batch of more rows in total and back: every
+    call solves the batch it is given (a cached launch sequence holds the
+    workspace layout of the row count it was captured for, so the row count
+    is part of its key)."""
+    import torch
+    s1 = np.array([300, 5000, 40, 1200], dtype=np.int64)
+    s2 = np.array([60000, 5000, 70000, 33], dtype=np.int64)
+    max_rows = int(max(s1.max(), s2.max()))
+    need = pcrp.workspace_size(len(s1), max_rows, which=2)
+    ws = torch.empty(need, dtype=torch.uint8, device=cuda)
+    opts = pcrp.Opts(workspace=ws.data_ptr(), workspace_bytes=need)
+    t = [torch.zeros(int(s2.sum()), dtype=torch.float64, device=cuda) for _ in range(6)]
+    off = torch.empty(len(s1) + 1, dtype=torch.int64, device=cuda)
+    for sizes, seed in ((s1, 41), (s2, 42), (s1, 43)):
+        arrs, offs = ragged_batch(sizes, seed)
+        for u, v in zip(t, arrs):
+            u[: len(v)].copy_(torch.from_numpy(v))
+        off.copy_(torch.from_numpy(offs))
+        pcrp.solve_ragged(*t, off, len(sizes), max_rows, mode=mode, opts=opts)
+        torch.cuda.synchronize()
+        x = t[5][: int(offs[-1])].cpu().numpy()
+        if mode == 0:
+            assert_bitexact(x, O.ragged(*arrs, offs[:-1], sizes, kind="pcr"), f"batch {list(sizes)}")
+        else:
+            xg = O.ragged(*arrs, offs[:-1], sizes, kind="ge")
+            for k in range(len(sizes)):
+                sl = slice(offs[k], offs[k + 1])
+                assert O.fwd_err(x[sl], xg[sl], 1, int(sizes[k])) <= 1e-12, (list(sizes), k)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
 def test_ragged_runs_in_the_workspace_it_asks_for(cuda, mode):
     """A caller-owned workspace of pcrp_workspace_size(nsys, max_rows,
     which=2) bytes is enough for either mode."""
