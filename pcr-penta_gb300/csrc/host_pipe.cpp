@@ -134,6 +134,7 @@ extern "C" pcrp_status pcrp_solve_host(const double* a, const double* b, const d
     ce = cudaEventRecord(E[0], st);
     for (int k = 0; k < 2 && ce == cudaSuccess; k++) ce = cudaStreamWaitEvent(S[k], E[0], 0);
     if (ce != cudaSuccess) return cuda_error(ce, "pcrp_solve_host: stream join");
+    pcrp_status failed = PCRP_OK;                 // the first error, after which nothing more is queued
     int64_t j0 = 0, next = first;
     for (int64_t q = 0; j0 < m; q++, j0 += next, next = std::min(3 * next, chunk)) {
         const int64_t mc = std::min(next, m - j0);
@@ -144,18 +145,22 @@ extern "C" pcrp_status pcrp_solve_host(const double* a, const double* b, const d
         for (int k = 0; k < 6; k++) dv[k] = src[k] ? base + (size_t)k * chunk * n : nullptr;
         for (int k = 0; k < 6 && ce == cudaSuccess; k++)
             if (src[k]) ce = copy_chunk(dv[k], src[k], j0, mc, m, n, layout, true, s);
-        if (ce != cudaSuccess) return cuda_error(ce, "pcrp_solve_host: copy in");
+        if (ce != cudaSuccess) { failed = cuda_error(ce, "pcrp_solve_host: copy in"); break; }
         rc = precision == 0
                  ? f64_solve(dv[0], dv[1], dv[2], dv[3], dv[4], dv[5], mc, n, layout, &so, s, false, false, who)
                  : pcrp_solve_mixed(dv[0], dv[1], dv[2], dv[3], dv[4], dv[5], mc, n, layout, tol, max_sweeps, &so,
                                     (pcrp_stream)s, nullptr);
-        if (rc != PCRP_OK) return rc;
+        if (rc != PCRP_OK) { failed = rc; break; }
         ce = copy_chunk(y, dv[5], j0, mc, m, n, layout, false, s);
-        if (ce != cudaSuccess) return cuda_error(ce, "pcrp_solve_host: copy out");
+        if (ce != cudaSuccess) { failed = cuda_error(ce, "pcrp_solve_host: copy out"); break; }
     }
+    // The caller's stream waits for the internal streams on every path, an
+    // error included: copies from and to the caller's host arrays may already
+    // be queued, and the caller must not reuse those arrays before they end.
     ce = cudaEventRecord(E[1], S[0]);
     if (ce == cudaSuccess) ce = cudaEventRecord(E[2], S[1]);
     if (ce == cudaSuccess) ce = cudaStreamWaitEvent(st, E[1], 0);
     if (ce == cudaSuccess) ce = cudaStreamWaitEvent(st, E[2], 0);
+    if (failed != PCRP_OK) return failed;         // (its message stays the last error)
     return cuda_error(ce, "pcrp_solve_host: stream join");
 }

@@ -130,8 +130,19 @@ def _check(rc: int, func: str) -> None:
         raise PcrpError(rc, func, last_error())
 
 
-def _ptr(x) -> Optional[int]:
-    """Raw device pointer of a CUDA tensor (float64, contiguous) or an int."""
+def _check_tensor(x, count: int, dtype: str) -> None:
+    # the library reads count elements of this type through the raw pointer
+    if str(x.dtype).replace("torch.", "") != dtype:
+        raise TypeError(f"expected a {dtype} tensor, got {x.dtype}")
+    if not x.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    if x.numel() < count:
+        raise ValueError(f"tensor of {x.numel()} elements where {count} are read")
+
+
+def _ptr(x, count: int = 0, dtype: str = "float64") -> Optional[int]:
+    """Raw device pointer of a CUDA tensor (contiguous, of `dtype`, at least
+    `count` elements) or an int (an address, taken as it is)."""
     if x is None:
         return None
     if isinstance(x, int):
@@ -139,10 +150,13 @@ def _ptr(x) -> Optional[int]:
     if hasattr(x, "data_ptr"):
         if not x.is_cuda:
             raise ValueError("expected a CUDA tensor")
-        if not x.is_contiguous():
-            raise ValueError("expected a contiguous tensor")
+        _check_tensor(x, count, dtype)
         return x.data_ptr()
     raise TypeError(f"cannot take a device pointer of {type(x)}")
+
+
+def _count(m: int, n: int) -> int:
+    return m * n if m > 0 and n > 0 else 0
 
 
 def _stream(s) -> Optional[int]:
@@ -167,7 +181,7 @@ def solve_f64(a, b, c, d, e, y, m: int, n: int, layout: int = CONTIGUOUS,
               opts: Optional[Opts] = None, stream=None, path: str = "auto") -> None:
     """FP64 PCR-Penta solve in place on y (pcrp_solve_f64 / _small / _split)."""
     fn = {"auto": "pcrp_solve_f64", "small": "pcrp_solve_f64_small", "split": "pcrp_solve_f64_split"}[path]
-    rc = getattr(lib(), fn)(*[_ptr(v) for v in (a, b, c, d, e, y)], m, n, layout,
+    rc = getattr(lib(), fn)(*[_ptr(v, _count(m, n)) for v in (a, b, c, d, e, y)], m, n, layout,
                             _opts(opts), _stream(stream))
     _check(rc, fn)
 
@@ -175,7 +189,8 @@ def solve_f64(a, b, c, d, e, y, m: int, n: int, layout: int = CONTIGUOUS,
 def solve_f64_noalloc(a, b, c, d, e, y, m: int, n: int, layout: int = CONTIGUOUS, stream=None) -> None:
     """pcrp_solve_f64 without any device allocation (scratch is a fixed array
     inside the library; m*n <= 524288)."""
-    rc = lib().pcrp_solve_f64_noalloc(*[_ptr(v) for v in (a, b, c, d, e, y)], m, n, layout, _stream(stream))
+    rc = lib().pcrp_solve_f64_noalloc(*[_ptr(v, _count(m, n)) for v in (a, b, c, d, e, y)], m, n, layout,
+                                      _stream(stream))
     _check(rc, "pcrp_solve_f64_noalloc")
 
 
@@ -184,22 +199,29 @@ def solve_mixed(a, b, c, d, e, y, m: int, n: int, layout: int = CONTIGUOUS, tol:
                 report: bool = True) -> Optional[MixedInfo]:
     """FP32 PCR + FP64 refinement in place on y; returns the info when report=True."""
     info = MixedInfo() if report else None
-    rc = lib().pcrp_solve_mixed(*[_ptr(v) for v in (a, b, c, d, e, y)], m, n, layout, tol, max_sweeps,
+    rc = lib().pcrp_solve_mixed(*[_ptr(v, _count(m, n)) for v in (a, b, c, d, e, y)], m, n, layout, tol, max_sweeps,
                                 _opts(opts), _stream(stream), ctypes.byref(info) if info is not None else None)
     _check(rc, "pcrp_solve_mixed")
     return info
 
 
-def _host_ptr(x) -> Optional[int]:
+def _host_ptr(x, count: int = 0) -> Optional[int]:
+    """Address of a host array (numpy or CPU tensor: contiguous float64, at
+    least `count` elements) or an int (an address, taken as it is)."""
     if x is None:
         return None
     if hasattr(x, "ctypes"):
+        if str(x.dtype) != "float64":
+            raise TypeError(f"expected a float64 array, got {x.dtype}")
         if not x.flags.c_contiguous:
             raise ValueError("expected a contiguous array")
+        if x.size < count:
+            raise ValueError(f"array of {x.size} elements where {count} are read")
         return x.ctypes.data
     if hasattr(x, "data_ptr"):
         if x.is_cuda:
             raise ValueError("expected a host tensor")
+        _check_tensor(x, count, "float64")
         return x.data_ptr()
     return int(x)
 
@@ -209,19 +231,22 @@ def solve_host(a, b, c, d, e, y, m: int, n: int, layout: int = CONTIGUOUS, preci
     """Solve a batch held in host memory (numpy arrays or CPU tensors, float64):
     chunks stream through the GPU with copies overlapping solves (pcrp_solve_host).
     Asynchronous on `stream`; synchronise before reading y."""
-    rc = lib().pcrp_solve_host(*[_host_ptr(v) for v in (a, b, c, d, e, y)], m, n, layout, precision, tol,
+    rc = lib().pcrp_solve_host(*[_host_ptr(v, _count(m, n)) for v in (a, b, c, d, e, y)], m, n, layout, precision, tol,
                                max_sweeps, _opts(opts), _stream(stream))
     _check(rc, "pcrp_solve_host")
 
 
 def residual_f64(a, b, c, d, e, y, x, r, m: int, n: int, layout: int = CONTIGUOUS, stream=None) -> None:
-    rc = lib().pcrp_residual_f64(*[_ptr(v) for v in (a, b, c, d, e, y, x, r)], m, n, layout, _stream(stream))
+    rc = lib().pcrp_residual_f64(*[_ptr(v, _count(m, n)) for v in (a, b, c, d, e, y, x, r)], m, n, layout,
+                                 _stream(stream))
     _check(rc, "pcrp_residual_f64")
 
 
 def solve_ragged(a, b, c, d, e, y, offsets, nsys: int, max_rows: int, mode: int = 0,
                  tol: float = 1e-12, max_sweeps: int = 8, opts: Optional[Opts] = None, stream=None) -> None:
-    rc = lib().pcrp_solve_ragged(*[_ptr(v) for v in (a, b, c, d, e, y)], _ptr(offsets), nsys, max_rows,
+    # (the arrays' length is offsets[nsys], on the device: only their type is checked here)
+    rc = lib().pcrp_solve_ragged(*[_ptr(v) for v in (a, b, c, d, e, y)], _ptr(offsets, nsys + 1, "int64"),
+                                 nsys, max_rows,
                                  mode, tol, max_sweeps, _opts(opts), _stream(stream))
     _check(rc, "pcrp_solve_ragged")
 
@@ -289,14 +314,15 @@ def generate(kind: int, seed: int, m: int, n: int, layout: int = CONTIGUOUS, thr
 
 def generate_into(kind: int, seed: int, m: int, n: int, layout: int, arrs, threads: int = 0) -> None:
     """Fill six preallocated host float64 arrays (numpy or pinned CPU tensors)."""
-    ptrs = [v.ctypes.data if hasattr(v, "ctypes") else v.data_ptr() for v in arrs]
+    ptrs = [_host_ptr(v, _count(m, n)) for v in arrs]
     rc = lib().pcrp_generate(kind, seed, m, n, layout, *ptrs, threads)
     _check(rc, "pcrp_generate")
 
 
 def generate_device(kind: int, seed: int, m: int, n: int, layout: int, arrs, stream=None) -> None:
     """Fill six device float64 arrays with the same values as :func:`generate`."""
-    rc = lib().pcrp_generate_device(kind, seed, m, n, layout, *[_ptr(v) for v in arrs], _stream(stream))
+    rc = lib().pcrp_generate_device(kind, seed, m, n, layout, *[_ptr(v, _count(m, n)) for v in arrs],
+                                    _stream(stream))
     _check(rc, "pcrp_generate_device")
 
 

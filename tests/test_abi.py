@@ -207,3 +207,48 @@ def test_mixed_residual_host_ragged_argument_validation(built_lib):
     assert rg(1, 1, 1, 1, 1, 1, None, 8, 64, 0, 0.0, 0, None, None) == 1                        # null offsets
     assert rg(1, 1, 1, 1, 1, 1, 1, (1 << 24) + 1, 64, 1, 0.0, 0, None, None) == 1               # nsys > 2^24
     assert "out of range" in pcrp.last_error()
+
+
+def test_python_wrappers_check_type_and_length(built_lib):
+    """The ctypes wrappers refuse arrays the library would read past or
+    misread (wrong element type, fewer than m*n elements, not contiguous)
+    before any call into it."""
+    import torch
+
+    good = np.zeros(64, dtype=np.float64)
+    with pytest.raises(TypeError):
+        pcrp.solve_host(*([np.zeros(64, dtype=np.float32)] * 6), 4, 16)
+    with pytest.raises(ValueError):
+        pcrp.solve_host(*([good[:63]] * 6), 4, 16)
+    with pytest.raises(ValueError):
+        pcrp.solve_host(*([np.zeros(128)[::2]] * 6), 4, 16)
+    with pytest.raises(TypeError):
+        pcrp.generate_into(pcrp.GEN_DOMINANT, 1, 4, 16, pcrp.CONTIGUOUS, [torch.zeros(64, dtype=torch.float32)] * 6)
+    assert pcrp._host_ptr(good, 64) == good.ctypes.data
+
+    class FakeDeviceTensor:                 # what _ptr reads of a CUDA tensor, without a GPU
+        is_cuda = True
+
+        def __init__(self, dtype, numel):
+            self.dtype, self._numel = dtype, numel
+
+        def is_contiguous(self):
+            return True
+
+        def numel(self):
+            return self._numel
+
+        def data_ptr(self):
+            return 4096
+
+    assert pcrp._ptr(FakeDeviceTensor(torch.float64, 64), 64) == 4096
+    with pytest.raises(TypeError):
+        pcrp._ptr(FakeDeviceTensor(torch.float32, 64), 64)
+    with pytest.raises(ValueError):
+        pcrp._ptr(FakeDeviceTensor(torch.float64, 63), 64)
+    with pytest.raises(TypeError):
+        pcrp.solve_ragged(*([FakeDeviceTensor(torch.float64, 64)] * 6), FakeDeviceTensor(torch.int32, 5), 4, 16)
+    with pytest.raises(ValueError):
+        pcrp.solve_ragged(*([FakeDeviceTensor(torch.float64, 64)] * 6), FakeDeviceTensor(torch.int64, 4), 4, 16)
+    with pytest.raises(ValueError):
+        pcrp.solve_mixed(*([FakeDeviceTensor(torch.float64, 63)] * 6), 4, 16)
