@@ -292,12 +292,13 @@ pcrp_status pcrp_workspace_size(int64_t m, int64_t n, int32_t layout, int32_t wh
     *bytes = 0;
     if (m < 0 || n < 0) return set_error(PCRP_EINVAL, "pcrp_workspace_size: negative size");
     if (!valid_layout(layout)) return set_error(PCRP_EINVAL, "pcrp_workspace_size: bad layout %d", layout);
+    // (no solver accepts a batch this large; the sizes below would wrap)
+    if (n > 0 && m > (int64_t(1) << 52) / n) return set_error(PCRP_EINVAL, "pcrp_workspace_size: m*n too large");
     const F64Plan pl = f64_plan(opts, n);
     switch (which) {
     case 0: *bytes = f64_workspace_bytes(m, n, layout, pl, true); return PCRP_OK;
     case 1: *bytes = mixed_workspace_bytes(m, n, opts, 64, true, layout); return PCRP_OK;
     case 2:                                      // either mode of pcrp_solve_ragged: m systems of <= n rows
-        if (n > 0 && m > (int64_t(1) << 52) / n) return set_error(PCRP_EINVAL, "pcrp_workspace_size: m*n too large");
         *bytes = std::max(ragged_workspace_bytes(m, m * n), ragged_mixed_workspace_bound(m, n, opts));
         return PCRP_OK;
     default: return set_error(PCRP_EINVAL, "pcrp_workspace_size: unknown entry family %d", which);

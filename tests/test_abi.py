@@ -160,8 +160,10 @@ def test_workspace_size_ragged_family(built_lib):
     for which in (3, -1):
         with pytest.raises(pcrp.PcrpError):
             pcrp.workspace_size(4, 4096, which=which)
-    with pytest.raises(pcrp.PcrpError):
-        pcrp.workspace_size(1 << 40, 1 << 20, which=2)
+    for which in (0, 1, 2):                  # no family's size wraps around
+        with pytest.raises(pcrp.PcrpError):
+            pcrp.workspace_size(1 << 40, 1 << 20, which=which)
+    assert pcrp.workspace_size(1 << 20, 1 << 20, which=0) == 2 * 8 * 8 * (1 << 40)
 
 
 def test_mixed_residual_host_ragged_argument_validation(built_lib):
