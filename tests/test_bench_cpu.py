@@ -199,3 +199,45 @@ def test_autotune_header_ragged_defaults():
     old.pop("ragged_best")
     last = old["f64_best"][-1]["opts"]
     assert f"#define PCRP_TUNED_TILE_ROWS {last['tile_rows']} " in autotune.header_text(old)
+
+
+def test_autotune_mixed_candidates_time_the_general_passes(monkeypatch):
+    """The mixed table plans the general block-PCR passes, so every mixed
+    candidate runs with the windows off; a size class none of whose
+    candidates ran is an error, not a silent gap in the table.  (Timing and
+    solves are replaced by fakes: no GPU.)"""
+    import types
+    sys.path.insert(0, os.path.join(bench.ROOT, "pcr-penta_gb300"))
+    from pcrp import autotune
+    cands = list(autotune.mp_candidates())
+    assert cands and all(c["window_levels"] == -1 for c in cands)
+    assert all(c["smem_rows"] // 2 - 2 * ((1 << c["fuse_strides"]) - 1) >= 32 for c in cands)
+
+    fake_torch = types.SimpleNamespace(cuda=types.SimpleNamespace(get_device_name=lambda i: "fake",
+                                                                  empty_cache=lambda: None))
+    monkeypatch.setitem(sys.modules, "torch", fake_torch)
+
+    class FakeArray:
+        def clone(self):
+            return self
+
+        def copy_(self, other):
+            return self
+
+    monkeypatch.setattr(autotune, "_batch", lambda m, n, seed=1: [FakeArray() for _ in range(6)])
+    seen = []
+
+    def timeit(fn, reps=5, warm=1):
+        fn()
+        return 1.0 + len(seen) * 1e-3
+    monkeypatch.setattr(autotune, "_timeit", timeit)
+    monkeypatch.setattr(autotune, "solve_mixed", lambda *a, **k: seen.append(k["opts"].window_levels))
+    rec = autotune.tune(verbose=False, only="mixed")
+    assert set(seen) == {-1} and len(rec["mixed_best"]) == len(autotune.MP_CLASSES)
+    assert all(b["ms"] == min(r["ms"] for r in rec["mixed"] if r["n"] == b["n"]) for b in rec["mixed_best"])
+
+    def refuse(*a, **k):
+        raise RuntimeError("refused")
+    monkeypatch.setattr(autotune, "solve_mixed", refuse)
+    with pytest.raises(RuntimeError, match="no mixed candidate ran"):
+        autotune.tune(verbose=False, only="mixed")
